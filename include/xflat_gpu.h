@@ -1,0 +1,207 @@
+/*
+ * xflat_gpu.h -- C ABI of the GB300 implementation of XFLAT's per-radius-step
+ * hot path (bulb-model MA/MAA neutrino-neutrino Hamiltonian moment integral and
+ * the SU(2) evolution of every beam, driven by the reference's adaptive
+ * three-point stepper).
+ *
+ * The reference selects its physics and numerics modules at compile time
+ * (include/global.h:5-28) and binds them as free functions:
+ *   include/Phy.h:24-159   phy::init, calcAngleBins, calcDeltaLs, calc_Hvv,
+ *                          evolveHvv, evolveAvg, initBeam, freemem ...
+ *   include/Nmr.h:20-31    nmr::init, evolutionLoop, freemem
+ *   include/Fio.h:22-38    fio::init, fillInitData, dumpToFile, freemem
+ *   include/Matt.h:22-36   matt::init, getHm
+ *   include/Parser.h:9-28  Parser(configFile)
+ * This header replaces that contract with handle-based entry points.  All
+ * buffers crossing the ABI are host memory in the reference's NetCDF psi
+ * layout [theta][phi][prtcl][comp][ebin] (src/IO_f.cpp:280-288), copied
+ * synchronously; no device pointers and no C++ types cross it.  Every entry
+ * point returns an xf_status; none exits or traps.  Calls on one handle must
+ * come from one thread at a time; handles are independent.
+ */
+#ifndef XFLAT_GPU_H_
+#define XFLAT_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference has none: its hot functions are throw() and IO
+ * failures call exit(-10) (src/IO_f.cpp:88). */
+enum {
+    XF_OK = 0,
+    XF_EINVAL = 1,       /* bad argument or configuration */
+    XF_ECUDA = 2,        /* CUDA runtime error, or no usable GPU */
+    XF_ETIMEOUT = 3,     /* a bounded device-side wait ran out */
+    XF_ENAN = 4,         /* the step error became NaN (the reference would spin until Ts) */
+    XF_EIO = 5,          /* file could not be read or written */
+    XF_ENOMEM = 6,       /* device or host allocation failed */
+    XF_EUNSUPPORTED = 7  /* option not supported for this geometry/precision */
+};
+
+enum { XF_GEOM_MA = 0, XF_GEOM_MAA = 1 };
+enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
+
+/* Run configuration.  Fields carry the reference's Util:: values in the same
+ * internal units after the same parse-time conversions (src/Parser.cpp:40-123:
+ * energies in km^-1, dm2 in km^-2, luminosities in km^-2, nb0 x 1e15).
+ * Keys missing from a config file keep the xf_config_default() value (the
+ * reference leaves them uninitialized). */
+typedef struct xf_config {
+    int geometry;        /* XF_GEOM_*  (extension key "geometry= MA|MAA") */
+    int precision;       /* XF_PREC_*  (extension key "precision= fp64|mixed") */
+    int abins, pbins, ebins, flvs;
+    int has_matter;      /* hasMatter= */
+    int dump_mode;       /* dumpMode= (bit 1 snapshot file, bit 2 probability file) */
+    int Ts;              /* max iterations */
+    int Tn;              /* max wall seconds */
+    int new_file_step, sync_step;
+    int tstep1, itrstep1, tstep2, itrstep2;
+    int start_beam, end_beam;
+    double rstep1, rstep2;
+    double eps0, ksi, mu;
+    double R0, Rn, dr, max_dr;
+    double E0, E1;
+    double Ye, Rv, Mns, gs, S, hNS, nb0;
+    double theta, theta2, dm2;
+    double Lv[4], Tv[4], eta[4];
+    uint64_t seed;       /* extension key "seed=" */
+    double noise_amp;    /* extension key "noise_amp=" (0 = pure flavor states) */
+    char file_prefix[256];
+} xf_config;
+
+typedef struct xf_handle xf_handle;
+
+/* Options and results of xf_run (the replacement of nmr::evolutionLoop,
+ * src/Nmr.cpp:89-262). */
+typedef struct xf_run_opts {
+    long max_iters;        /* < 0: use cfg.Ts */
+    int device_control;    /* 1: accept/reject and dr control run on the GPU, no per-step host sync */
+    int iters_per_launch;  /* device_control: iterations captured per CUDA graph launch (default 16) */
+    int write_files;       /* 1: honour dump_mode through the NetCDF writer (host-driven loop only) */
+    int time_phases;       /* 1: time every phase kernel with CUDA events (see xf_phase_times) */
+    double r0, dr0;        /* starting radius and step; NaN -> cfg.R0 / cfg.dr */
+    double* log;           /* optional host buffer for accepted steps (itr, r_after, dr_used) */
+    long log_cap;          /* capacity of log in records */
+} xf_run_opts;
+
+typedef struct xf_run_stats {
+    long iterations;       /* counter_tot (src/Nmr.cpp:246) */
+    long accepted;         /* counter (src/Nmr.cpp:244) */
+    double r_end, dr_end;
+    double seconds;        /* wall time of the loop */
+    double last_max_err;
+    double device_ms;      /* CUDA-event time of the loop on the handle's stream */
+    long kernel_launches;  /* device kernels launched by this call */
+    long log_len;          /* accepted-step records written to opts->log */
+} xf_run_stats;
+
+/* Defaults: max_iters -1, device_control 0, iters_per_launch 16, r0/dr0 NaN. */
+int xf_run_opts_default(xf_run_opts* o);
+
+/* Called on every accepted step of a host-driven xf_run, in the place of
+ * fio::dumpToFile (src/Nmr.cpp:238): (user, itr, r_after, dr_used).  Return
+ * nonzero to stop the loop. */
+typedef int (*xf_step_cb)(void* user, long itr, double r, double dr);
+
+/* ---------------------------------------------------------------- config */
+/* Parser(configFile) (src/Parser.cpp:13-127). */
+int xf_config_default(xf_config* cfg);
+int xf_config_load(const char* path, xf_config* cfg);
+int xf_config_parse(const char* text, xf_config* cfg);
+const char* xf_strerror(int status);
+
+/* Host-only (no GPU needed): the tables of xf_tables, the matter term of
+ * xf_matter and the initial state of xf_create computed from a configuration
+ * (src/NBeam.cpp:138-209, src/Matt.cpp:58-64, src/NBeam.cpp:246-276). */
+int xf_host_tables(const xf_config* cfg, double* fv, double* hvac, double* LE, double* Ev);
+int xf_host_matter(const xf_config* cfg, double r, double* hm);
+int xf_host_initial_state(const xf_config* cfg, uint64_t seed, double amp, double* psi);
+
+/* ---------------------------------------------------------------- lifecycle */
+/* nbm::init + phy::init + nmr::init + matt::init (src/NBGroup.cpp:129-139;
+ * src/NBeam.cpp:138-209; src/Phy_MA.cpp:233-284; src/Phy_MAA.cpp:247-304;
+ * src/Nmr.cpp:48-70; src/Matt.cpp:22-29).  Beams start in pure flavor states
+ * (src/NBeam.cpp:246-276), plus seeded noise when cfg->noise_amp > 0. */
+int xf_create(const xf_config* cfg, xf_handle** out);
+/* phy::freemem / nmr::freemem / nbm::freemem (src/Phy_MA.cpp:290-302). */
+int xf_destroy(xf_handle* h);
+/* Message of the last failing call on this handle. */
+const char* xf_last_error(const xf_handle* h);
+/* nbeams = theta*phi*4 (phy::beamLen, src/Phy_MA.cpp:78). */
+int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins);
+/* Tuning and diagnostics, no reference counterpart: "threads" / "blocks" set
+ * the launch shape of the phase kernels (0 = default); "debug_psi3" = 1 makes
+ * the last phase also store U(h4, dl2) psi3 into psi3, as the reference's
+ * in-place stage S10 does (src/Nmr.cpp:191). */
+int xf_set_option(xf_handle* h, const char* name, double value);
+
+/* ---------------------------------------------------------------- state */
+/* fio::fillInitData / phy::initBeam (src/IO_f.cpp:197-250): psi0 <- psi and
+ * the cached energy moments S(psi0) are recomputed (src/Nmr.cpp:117-121). */
+int xf_set_state(xf_handle* h, const double* psi);
+/* Reads buffer `which` (0 = psi0, 1 = psi1, 3 = psi3, 4 = psi4) into psi. */
+int xf_get_state(xf_handle* h, int which, double* psi);
+/* Seeded initial noise (a,b) = (sqrt(1-e^2-n^2), e+i n) on psi0, the form of
+ * src/NBeam.cpp:260-275 with a counter-based generator. */
+int xf_set_noise(xf_handle* h, uint64_t seed, double amp);
+
+/* ---------------------------------------------------------------- tables */
+/* Energy tables fv[4][ebins], hvac[2*ebins], L/<E> per particle and <E>
+ * (src/NBeam.cpp:138-209, src/Fenergy.cpp:16-47, src/Phy_MA.cpp:280-282). */
+int xf_tables(const xf_handle* h, double* fv, double* hvac, double* LE, double* Ev);
+/* matt::getHm (src/Matt.cpp:58-64). */
+int xf_matter(const xf_handle* h, double r, double* hm);
+/* phy::calcAngleBins(r,0..2) + calcDeltaLs (src/Nmr.cpp:167-173) on the GPU;
+ * outputs [3][abins] each (sinb unused for MA). */
+int xf_angle_bins(xf_handle* h, double r, double dr, double* cosb, double* sinb, double* dcosb, double* dl);
+/* phy::calc_Hvv on buffer `which` at stage point pt after xf_angle_bins(r, dr)
+ * (src/Phy_MA.cpp:455-474, src/Phy_MAA.cpp:571-621); hvv[abins*pbins][4]. */
+int xf_calc_hvv(xf_handle* h, int which, int pt, double r, double dr, double* hvv);
+
+/* ---------------------------------------------------------------- stepping */
+/* One stepper iteration at (r, dr): stages S1..S11 and the error sweep of
+ * src/Nmr.cpp:153-206.  The candidate stays on the device; *max_err receives
+ * Max_err.  Returns XF_ENAN if Max_err is NaN. */
+int xf_step(xf_handle* h, double r, double dr, double* max_err);
+/* Accept the candidate: psi0 <-> psi4 (src/Nmr.cpp:227-233). */
+int xf_accept(xf_handle* h);
+/* Full loop with the reference's termination, accept/reject and dr control
+ * (src/Nmr.cpp:89-262).  cb may be NULL.  opts may be NULL (defaults). */
+int xf_run(xf_handle* h, const xf_run_opts* opts, xf_step_cb cb, void* user, xf_run_stats* stats);
+/* Forced steps: applies n accepted steps (r_before[i], dr[i]) in order, as
+ * the reference's loop did; used to replay a recorded step sequence. */
+int xf_replay(xf_handle* h, const double* r_before, const double* dr, long n);
+/* Average CUDA-event time per launch (ms) of the three phase kernels over the
+ * last xf_run with time_phases = 1: out[0..2]; counts[0..2] launches timed. */
+int xf_phase_times(const xf_handle* h, double* out, long* counts);
+
+/* ---------------------------------------------------------------- output */
+/* Per-beam survival probabilities written to the reference's Probability file:
+ * sum_e fv*(ar^2+ai^2), with the fv of beam i*4 + p%2 (src/IO_f.cpp:341-351);
+ * out[theta*phi][4]. */
+int xf_survival(xf_handle* h, double* out);
+
+/* ---------------------------------------------------------------- batch */
+/* Many independent simulations with per-instance adaptive steps, advanced
+ * together by the same phase kernels (one launch per phase covers every
+ * instance), captured in CUDA graphs.  All configs must share geometry (MA)
+ * and precision. */
+typedef struct xf_batch xf_batch;
+int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out);
+int xf_batch_destroy(xf_batch* b);
+const char* xf_batch_last_error(const xf_batch* b);
+int xf_batch_dims(const xf_batch* b, int inst, int* nbeams, int* ebins);
+int xf_batch_set_state(xf_batch* b, int inst, const double* psi);
+int xf_batch_get_state(xf_batch* b, int inst, double* psi);
+/* Advance every unfinished instance by up to max_iters iterations (< 0: each
+ * instance's Ts); per-instance results in iters/accepted/r_end (may be NULL). */
+int xf_batch_run(xf_batch* b, long max_iters, long* iters, long* accepted, double* r_end, double* seconds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XFLAT_GPU_H_ */

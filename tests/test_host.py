@@ -1,0 +1,110 @@
+"""Host-side logic of the product (C++ through the C ABI, no GPU calls):
+config parsing with the reference's units, tables, matter, initial state, and
+the exported symbol set."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import xflat_gb300 as xg
+from xflat_gb300 import _abi
+from helpers import CONFIGS, TempConfig, derive, golden, golden_names, noise_state
+from oracle.port import Port
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _abi.load()
+    names = _abi.header_symbols()
+    assert len(names) > 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_config_units_and_keys():
+    c = xg.Parser(os.path.join(CONFIGS, "config0_ma.txt"))
+    MEV, EV2, ERG = 5.067731161976211e+15, 2.568189913006477e+19, 1.053613095584080e+16
+    assert c.abins == 256 and c.ebins == 64 and c.pbins == 1 and c.flvs == 2
+    assert c.E0 == 1 * MEV and c.E1 == 60 * MEV
+    assert c.dm2 == -3e-3 * EV2
+    assert c.theta2 == 0.2
+    assert list(c.Lv) == [1e51 * ERG] * 4
+    assert c.Tv[0] == 2.76 * MEV and c.Tv[3] == 6.26 * MEV
+    assert c.eps0 == 1e-9 and c.ksi == 0.94 and c.R0 == 10 and c.Rn == 300
+    assert c.geometry == xg.XF_GEOM_MA and c.precision == xg.XF_PREC_FP64
+    assert c.seed == 1 and c.noise_amp == 1e-7
+    c3 = xg.Parser(os.path.join(CONFIGS, "config3_maa.txt"))
+    assert c3.geometry == xg.XF_GEOM_MAA and c3.pbins == 64
+    c2 = xg.Parser(os.path.join(CONFIGS, "config2_ma_mixed.txt"))
+    assert c2.precision == xg.XF_PREC_MIXED
+
+
+def test_config_reference_syntax():
+    # comments, unknown keys, trailing comments, nb0 scaling, int keys parsed like istream >> int
+    text = "# c\n\nfoo= 3\nnb0= 1.63E+36 # cm^-3\nAbins= 12\nEbins= 7\nt_step1= 300000.\nfilePrefix= abc\n"
+    c = xg.Config.from_text(text)
+    assert c.nb0 == 1.63e36 * 1e15
+    assert c.abins == 12 and c.ebins == 7 and c.tstep1 == 300000
+    assert c.file_prefix == b"abc"
+    with pytest.raises(xg.XflatError):
+        xg.Config.from_text("geometry= XYZ\n")
+    with pytest.raises(xg.XflatError):
+        xg.Parser("/nonexistent/config.txt")
+
+
+@pytest.mark.parametrize("name", golden_names("probe"))
+def test_host_tables_match_reference(name):
+    g = golden(name)
+    c = xg.Config.from_text(g["config"])
+    lib = _abi.load()
+    ne = c.ebins
+    fv, hv, le, ev = np.empty(4 * ne), np.empty(2 * ne), np.empty(4), np.empty(4)
+    dp = _abi.c_double_p
+    assert lib.xf_host_tables(ctypes.byref(c.raw), fv.ctypes.data_as(dp), hv.ctypes.data_as(dp),
+                              le.ctypes.data_as(dp), ev.ctypes.data_as(dp)) == 0
+    np.testing.assert_allclose(fv, g["probe_fv"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(hv, g["probe_hvac"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(le, g["probe_LE"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(ev, g["probe_Ev"], rtol=1e-14, atol=0)
+    r, dr = c.R0, c.dr
+    hm = []
+    for x in (r, r + .5 * dr, r + dr):
+        o = ctypes.c_double()
+        assert lib.xf_host_matter(ctypes.byref(c.raw), x, ctypes.byref(o)) == 0
+        hm.append(o.value)
+    np.testing.assert_allclose(hm, g["probe_hm"], rtol=1e-15, atol=0)
+
+
+def test_matter_profile_is_the_baseline_lambda():
+    """lambda(r) = 1e3 (10/r)^3 km^-1 with the workload's matter keys; hm = lambda/2."""
+    c = xg.Parser(os.path.join(CONFIGS, "config0_ma.txt"))
+    lib = _abi.load()
+    for r in (10., 50., 300.):
+        o = ctypes.c_double()
+        lib.xf_host_matter(ctypes.byref(c.raw), r, ctypes.byref(o))
+        assert abs(2 * o.value / (1e3 * (10. / r) ** 3) - 1) < 1e-5
+
+
+@pytest.mark.parametrize("geom,a,p,e", [("config0_ma.txt", 13, 1, 21), ("config3_maa.txt", 5, 3, 9)])
+def test_host_initial_state_matches_numpy_and_oracle(geom, a, p, e):
+    text = derive(geom, Abins=a, Pbins=p, Ebins=e)
+    c = xg.Config.from_text(text)
+    nb = a * (p if c.geometry == 1 else 1) * 4
+    psi = np.empty(nb * 4 * e)
+    assert _abi.load().xf_host_initial_state(ctypes.byref(c.raw), 7, 1e-6, psi.ctypes.data_as(_abi.c_double_p)) == 0
+    ref = noise_state(nb, e, 7, 1e-6)
+    assert np.array_equal(psi.reshape(nb, 4, e), ref)
+    with TempConfig(text) as path:
+        port = Port(path)
+    port.noise(7, 1e-6)
+    assert np.array_equal(port.get_state(0), ref)
+
+
+def test_invalid_config_is_rejected_without_gpu_work():
+    lib = _abi.load()
+    c = xg.Config.from_text(derive("config0_ma.txt", Abins=0))
+    h = ctypes.c_void_p()
+    assert lib.xf_create(ctypes.byref(c.raw), ctypes.byref(h)) == _abi.XF_EINVAL
+    c = xg.Config.from_text(derive("config0_ma.txt", Flvs=3))
+    assert lib.xf_create(ctypes.byref(c.raw), ctypes.byref(h)) == _abi.XF_EUNSUPPORTED
+    assert lib.xf_create(None, ctypes.byref(h)) == _abi.XF_EINVAL

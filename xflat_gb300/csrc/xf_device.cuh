@@ -1,0 +1,83 @@
+// Device-side types shared by the kernels and the host engine.
+//
+// Data layout in HBM (one handle = one simulation):
+//   state buffers  psi0, psi1, psi3, psi4: [beam][comp][epad] (comp = ar, ai,
+//                  br, bi; epad = ebins rounded up to a multiple of 32; padding
+//                  bins hold zeros and have zero weight).  This is the
+//                  reference's NetCDF psi layout with the energy axis padded,
+//                  so a warp reads 32 consecutive energies of one component.
+//   per-beam sums  S0, S4: [beam][4] energy moments sum_e fv*rho(psi) of psi0
+//                  and of the candidate (the reference's NBeam::hSumMat).
+//   tables         fv[4][epad], hvac[2][epad], angle grids [abins], azimuth
+//                  grids [pbins], geometry at the three stage points
+//                  geo[4][3][abins] (cos, sin, dcos, dl).
+//   control block  Ctl: radius, step, matter terms, the angular moments J of
+//                  every stage, the step error and the loop counters.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xf {
+
+constexpr int kNJ = 16;        // moment slots: MA uses J0[4], J1[4]; MAA J0, Jx, Jy, Jz [4] each
+constexpr int kPartStride = 32;  // doubles per block in the partial-sum buffer
+
+enum Phase { PH_A = 0, PH_B = 1, PH_C = 2, PH_MOM = 3 };
+
+struct Ctl {
+    double r, dr;         // current iteration
+    double hm[3];         // matter term at r, r+dr/2, r+dr
+    double J0[kNJ];       // moments of psi0 at stage point 0
+    double JA1[kNJ];      // psi1 = U(h0, dl1) psi0 at point 2   (S2 -> S3)
+    double JA3[kNJ];      // psi3 = U(h0, dl0) psi0 at point 1   (S6 -> S7)
+    double JB4[kNJ];      // psi4 = U(h3, dl1) psi0 at point 2   (S8 -> S9)
+    double JC[kNJ];       // candidate at point 2 (J0 of the next iteration if accepted)
+    double JM[kNJ];       // scratch result of the standalone moment kernel
+    double max_err;       // Max_err = sqrt(max_b err_b)   (src/Nmr.cpp:195-206)
+    double* psi0;         // roles swapped on accept (src/Nmr.cpp:231-233)
+    double* psi4;
+    double* S0;
+    double* S4;
+    unsigned int ticket[4];  // last-block tickets per phase
+    int done;             // device control: no further iterations
+    int nan_seen;
+    long long iters;      // counter_tot
+    long long accepted;   // counter
+    long long max_iters;  // Ts
+    long long log_len;    // accepted-step records written to the log
+};
+
+// Kernel parameters (passed by value).
+struct Dev {
+    int geom;             // 0 MA, 1 MAA
+    int nbeams, A, P, ne, epad;
+    const double* fv;     // [4][epad]
+    const double* hvac;   // [2][epad]: h00 part, then h01 real part
+    const double* cos2R;  // [A]
+    const double* dcos2R; // [A]
+    const double* sinR;   // [A]
+    const double* cosphi; // [P]
+    const double* sinphi; // [P]
+    double* geo;          // [4][3][A]
+    double* psi1;
+    double* psi3;
+    double* partials;     // [grid][kPartStride]
+    double* log;          // accepted-step log [cap][3] (device control), may be null
+    long long log_cap;
+    Ctl* ctl;
+    double LE[4];
+    double kappa;
+    double Rv;
+    // step control (src/Nmr.cpp:227-249)
+    double eps0, ksi, maxdr, Rn;
+    // matter profile (src/Matt.cpp:22-64)
+    int has_matter;
+    double mat_coeff, nbfar, nb0, hNS;
+    int device_control;   // phase C runs the accept/reject/dr controller
+    int debug_psi3;       // phase C also stores U(h4, dl2) psi3 into psi3 (the reference's S10 result)
+};
+
+// Geometry table accessors: q = 0 cos, 1 sin, 2 dcos, 3 dl.
+__host__ __device__ inline int geo_idx(int q, int pt, int ang, int A) { return (q * 3 + pt) * A + ang; }
+
+}  // namespace xf

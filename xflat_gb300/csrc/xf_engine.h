@@ -1,0 +1,83 @@
+// The handle behind the C ABI.  Internal to the library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "xf_device.cuh"
+#include "xf_kernels.h"
+#include "xf_physics.h"
+#include "xflat_gpu.h"
+
+namespace xf {
+struct Mixed;  // mixed-precision state (xf_mixed.cu)
+}
+
+struct xf_handle {
+    xf_config cfg{};
+    xf::Tables tab;
+    int device = 0;
+    int A = 0, P = 1, ne = 0, epad = 0, nbeams = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[7] = {};
+    std::vector<cudaEvent_t> tev;  // timing events captured into graphs
+
+    // device memory
+    double* d_fv = nullptr;
+    double* d_hvac = nullptr;
+    double* d_cos2R = nullptr;
+    double* d_dcos2R = nullptr;
+    double* d_sinR = nullptr;
+    double* d_cosphi = nullptr;
+    double* d_sinphi = nullptr;
+    double* d_geo = nullptr;
+    double* d_partials = nullptr;
+    double* d_hvv = nullptr;
+    double* d_Sscratch = nullptr;
+    double* d_psi[4] = {};  // storage for psi0, psi1, psi3, psi4 (roles of 0 and 3 swap)
+    double* d_S[2] = {};    // per-beam energy sums of psi0 / candidate
+    double* d_log = nullptr;
+    long log_cap_dev = 0;
+    xf::Ctl* d_ctl = nullptr;
+    xf::Ctl* h_ctl = nullptr;  // pinned mirror
+    double* h_in = nullptr;    // pinned r, dr, hm[3]
+
+    xf::Dev dev{};
+    xf::Shape shape;
+    xf::Mixed* mixed = nullptr;
+
+    // host bookkeeping
+    bool j0_valid = false;
+    double j0_r = 0.;
+    double last_r = 0., last_dr = 0.;
+    int debug_psi3 = 0;
+    int time_phases = 0;
+    double phase_ms[3] = {0., 0., 0.};
+    long phase_n[3] = {0, 0, 0};
+    long launches = 0;
+    std::string err;
+
+    struct GraphEntry {
+        int k;
+        bool timed;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+    cudaGraphExec_t step_exec = nullptr;
+
+    int fail(int code, const std::string& msg);
+    int init(const xf_config& c);
+    void release();
+    int pull_ctl();
+    int set_state(const double* psi);
+    int get_state(int which, double* psi);
+    int push_inputs(double r, double dr);
+    int refresh_j0(double r);
+    int step(double r, double dr, double* max_err);
+    int accept();
+    int run_host(const xf_run_opts& o, xf_step_cb cb, void* user, xf_run_stats& s);
+    int run_device(const xf_run_opts& o, xf_run_stats& s);
+    int get_graph(int k, bool timed, cudaGraphExec_t* out);
+    int dump_files(long itr, double r, double dr);
+};

@@ -1,0 +1,26 @@
+// Launch wrappers for the FP64 kernels (xf_kernels.cu).  Every wrapper only
+// enqueues work on `st`; errors surface through cudaGetLastError().
+#pragma once
+#include <cuda_runtime.h>
+
+#include "xf_device.cuh"
+
+namespace xf {
+
+struct Shape {
+    int threads = 256;   // threads per block (multiple of 32)
+    int blocks = 0;      // grid size of the phase kernels
+};
+
+// Grid-size limit used to size the partial-sum buffer.
+int max_phase_blocks(int nbeams, int threads);
+Shape default_shape(int nbeams, int epad);
+
+void launch_geometry(const Dev& d, cudaStream_t st);
+void launch_esum(const Dev& d, const double* psi, double* S, cudaStream_t st);
+void launch_moments(const Dev& d, const double* S, int pt, double* Jout, cudaStream_t st);
+void launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st);
+void launch_accept(const Dev& d, cudaStream_t st);
+void launch_hvv_eval(const Dev& d, const double* J, int pt, double* hvv, cudaStream_t st);
+
+}  // namespace xf
