@@ -185,6 +185,12 @@ int xf_phase_times(const xf_handle* h, double* out, long* counts);
  * out[theta*phi][4]. */
 int xf_survival(xf_handle* h, double* out);
 
+/* ---------------------------------------------------------------- measurement */
+/* No reference counterpart.  Measures this GPU's FP64 FMA throughput with a
+ * register-resident DFMA loop (8 independent chains per thread, grid of 8
+ * blocks per SM) for about `ms` milliseconds: *tflops = 2 flops per FMA. */
+int xf_probe_fp64_peak(double ms, double* tflops);
+
 /* ---------------------------------------------------------------- batch */
 /* Many independent simulations with per-instance adaptive steps, advanced
  * together by the same phase kernels (one launch per phase covers every

@@ -145,8 +145,14 @@ class Simulation:
 
     fillInitData = set_state
 
-    def get_state(self, which=0):
-        out = np.empty(self.nbeams * 4 * self.ebins)
+    def get_state(self, which=0, out=None):
+        """Reads buffer `which` (0 psi0, 1 psi1, 3 psi3, 4 psi4); `out` may be a
+        caller-owned (e.g. pinned) float64 buffer of nbeams*4*ebins values."""
+        n = self.nbeams * 4 * self.ebins
+        if out is None:
+            out = np.empty(n)
+        elif out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
+            raise XflatError(XF_EINVAL, "out must be a contiguous float64 buffer of %d values" % n)
         self._c(self.lib.xf_get_state(self.h, int(which), _dp(out)), "xf_get_state")
         return out.reshape(self.state_shape)
 

@@ -454,19 +454,23 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     h_ctl->done = (r < cfg.Rn && Ts > 0) ? 0 : 1;
     for (int i = 0; i < 4; ++i) h_ctl->ticket[i] = 0;
     XF_CUDA(this, cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
-    cudaGraphExec_t ex;
-    if ((rc = get_graph(k, o.time_phases != 0, &ex))) return rc;
     const double t0 = now_s();
     XF_CUDA(this, cudaEventRecord(ev[4], st));
     long long prev_iters = 0;
     while (!h_ctl->done) {
         if ((long)(now_s() - t0) >= cfg.Tn) break;
+        // the last launch is sized to the remaining iteration budget, so that no
+        // graph node runs only to find the loop finished
+        const long long left = Ts - prev_iters;
+        const int kk = (int)std::min<long long>(k, std::max<long long>(1, left));
+        cudaGraphExec_t ex;
+        if ((rc = get_graph(kk, o.time_phases != 0, &ex))) return rc;
         XF_CUDA(this, cudaGraphLaunch(ex, st));
         XF_CUDA(this, cudaStreamSynchronize(st));
         const long long ran = h_ctl->iters - prev_iters;
         launches += 4 * ran;
         if (o.time_phases) {
-            for (long long i = 0; i < ran && i < k; ++i)
+            for (long long i = 0; i < ran && i < kk; ++i)
                 for (int ph = 0; ph < 3; ++ph) {
                     float ms;
                     XF_CUDA(this, cudaEventElapsedTime(&ms, tev[6 * i + 2 * ph], tev[6 * i + 2 * ph + 1]));
