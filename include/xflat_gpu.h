@@ -185,6 +185,24 @@ int xf_phase_times(const xf_handle* h, double* out, long* counts);
  * out[theta*phi][4]. */
 int xf_survival(xf_handle* h, double* out);
 
+/* No counterpart in the reference.  phy::calc_Hvv for callers that cannot
+ * allocate device memory (their device memory is owned and budgeted up front
+ * by another allocator, or their per-step loop must not pay cudaMalloc's
+ * implicit device synchronisation).  Every pointer except LE (host, 4
+ * doubles) is device memory the caller owns: psi [abins*pbins*4][4][epad]
+ * (epad >= ebins), fv [4][epad], cosb/sinb/dcosb [abins] at the stage point
+ * (sinb, cosphi, sinphi [pbins] only for MAA), hvv [abins*pbins][4] out;
+ * kappa is the Hamiltonian coefficient.  Allocates nothing: its scratch is a
+ * fixed 2.06 MiB device array inside the library, which limits it to
+ * abins*pbins*4 <= 65536 beams (larger sizes return XF_EINVAL).  The first call
+ * on a device looks that array up (make it before any stream capture); calls
+ * that overlap on the GPU race on the shared array.  Work is queued on
+ * `stream` (a cudaStream_t, NULL for the default stream). */
+int xf_calc_hvv_static(int geometry, int abins, int pbins, int ebins, int epad, const double* psi,
+                       const double* fv, const double* cosb, const double* sinb, const double* dcosb,
+                       const double* cosphi, const double* sinphi, const double* LE, double kappa,
+                       double* hvv, void* stream);
+
 /* ---------------------------------------------------------------- measurement */
 /* No reference counterpart.  Measures this GPU's FP64 FMA throughput with a
  * register-resident DFMA loop (8 independent chains per thread, grid of 8

@@ -90,6 +90,10 @@ PROTOTYPES = {
     "xf_phase_times": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_long_p]),
     "xf_survival": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "xf_probe_fp64_peak": (ctypes.c_int, [ctypes.c_double, c_double_p]),
+    "xf_calc_hvv_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double_p,
+                                          ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
     "xf_batch_create": (ctypes.c_int, [ctypes.POINTER(XfConfig), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "xf_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "xf_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
