@@ -237,6 +237,7 @@ def ours(args, rank, world, dist):
     # inputs resident in HBM (4 state buffers of 134 MB each: larger than L2)
     w = sim.evolutionLoop(max_iters=max(3, args.warmup), device_control=True, iters_per_launch=16)
     r0, dr0 = w["r_end"], w["dr_end"]
+    psi_start = sim.get_state(0).copy()
     if dist:
         dist.barrier()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
@@ -247,6 +248,12 @@ def ours(args, rank, world, dist):
     phase_ms, phase_n = sim.phase_times()
     secs = st["device_ms"] * 1e-3
     units = bins * st["iterations"]
+    psi_fp64_end = sim.get_state(0).copy()
+    surv_fp64 = sim.survival()
+
+    # --- mixed precision on the same workload (FP32 rotations and compensated
+    # FP32 state, FP64 reductions/control): same start state, same K steps
+    mixed = mixed_leg(xg, text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
 
     # --- end to end through the C ABI with host buffers: state H2D from pinned
     # memory, the host-driven reference loop (per step: r, dr and the three
@@ -309,6 +316,7 @@ def ours(args, rank, world, dist):
                                   "frac": hbm_achieved / hbm_peak if hbm_peak else None,
                                   "algorithmic_bytes_per_bin": PHASE_BYTES[dom]}},
         "phases_ms": {p: phase_ms[i] for i, p in enumerate("ABC")},
+        "variants": {"fp64": {"value": value, "unit": UNIT}, "mixed": mixed},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": (state_bytes + 40 * e["iterations"]) /
                 max(1, e["iterations"]), "d2h_bytes_per_step": (state_bytes + 8 * e["iterations"]) /
@@ -318,6 +326,32 @@ def ours(args, rank, world, dist):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def pee(psi):
+    """P_ee(E) = |a(E)|^2 of the nu_e beams (particle index 0)."""
+    x = psi[0::4]
+    return x[:, 0] ** 2 + x[:, 1] ** 2
+
+
+def mixed_leg(xg, text, psi_start, r0, dr0, steps, bins, psi_fp64_end, surv_fp64, st64):
+    """Mixed-precision run of the same K steps from the same state; accuracy
+    against the FP64 run: max |dP_ee(E)| over every nu_e beam and max
+    per-beam survival-probability error (src/IO_f.cpp:341-351 quantity)."""
+    import numpy as np
+    m = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= mixed")))
+    m.set_state(psi_start)
+    out = m.evolutionLoop(max_iters=steps, device_control=True, iters_per_launch=min(16, steps), r0=r0, dr0=dr0)
+    res = {"value": bins * out["iterations"] / (out["device_ms"] * 1e-3), "unit": UNIT,
+           "ms_per_step": out["device_ms"] / max(1, out["iterations"]), "iterations": out["iterations"],
+           "accepted": out["accepted"], "accepted_fp64": st64["accepted"],
+           "workload": "same as the FP64 line, precision= mixed (FP32 rotations and compensated FP32 state; "
+                       "FP64 moment reduction, error estimate, control, renormalisation)"}
+    if out["accepted"] == st64["accepted"]:
+        res["max_dPee_vs_fp64"] = float(np.max(np.abs(pee(m.get_state(0)) - pee(psi_fp64_end))))
+        res["max_dsurvival_vs_fp64"] = float(np.max(np.abs(m.survival() - surv_fp64)))
+    m.close()
+    return res
 
 
 def lib_peak(lib):

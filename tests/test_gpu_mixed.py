@@ -1,0 +1,106 @@
+"""Mixed-precision path (FP32 rotations and compensated FP32 state; FP64
+reductions, error estimate, control and renormalisation) against the FP64 path.
+Bars: P_ee(E) of every nu_e beam within 1e-5 of FP64 over the windows below
+(the spec bar for the mixed path); the step error within 2e-2 relative at step sizes near the adaptive ones."""
+import numpy as np
+import pytest
+
+import xflat_gb300 as xg
+from helpers import derive, noise_state
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(text, seed=1, amp=1e-7):
+    a = xg.Simulation(xg.Config.from_text(text))
+    b = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= mixed")))
+    psi = noise_state(a.nbeams, a.ebins, seed, amp)
+    a.set_state(psi)
+    b.set_state(psi)
+    return a, b
+
+
+def pee(psi):
+    """P_ee(E) = |a(E)|^2 of the nu_e beams (particle index 0)."""
+    x = psi[0::4]
+    return x[:, 0] ** 2 + x[:, 1] ** 2
+
+
+# radii with step sizes near the adaptive ones of the config-0 physics
+@pytest.mark.parametrize("r,dr", [(10.0, 1.3e-8), (20.0, 1.2e-5), (50.0, 1.5e-4), (200.0, 5e-3)])
+def test_error_estimate_matches_fp64(r, dr):
+    a, b = _pair(derive("config0_ma.txt", Abins=32, Ebins=64))
+    me64 = a.step(r, dr)
+    me32 = b.step(r, dr)
+    assert abs(me32 - me64) <= 2e-2 * me64, (me32, me64)
+    # the candidate agrees with the FP64 candidate to FP32 precision of the increment
+    inc = np.max(np.abs(a.get_state(4) - a.get_state(0)))
+    assert np.max(np.abs(b.get_state(4) - a.get_state(4))) <= 2e-7 * inc + 1e-13
+
+
+def test_error_estimate_matches_fp64_maa():
+    a, b = _pair(derive("config3_maa.txt", Abins=16, Pbins=8, Ebins=32), 3, 1e-6)
+    for r, dr in [(12.0, 1.4e-6), (60.0, 2e-4)]:
+        me64, me32 = a.step(r, dr), b.step(r, dr)
+        assert abs(me32 - me64) <= 2e-2 * me64, (r, me32, me64)
+
+
+@pytest.mark.parametrize("r0,iters", [(10.0, 400), (50.0, 300)])
+def test_free_running_window_vs_fp64(r0, iters):
+    text = derive("config0_ma.txt", Abins=64, Ebins=64, R0=r0, dr="1e-6")
+    a, b = _pair(text)
+    oa = a.evolutionLoop(max_iters=iters)
+    ob = b.evolutionLoop(max_iters=iters)
+    assert abs(oa["accepted"] - ob["accepted"]) <= 2
+    assert abs(oa["r_end"] - ob["r_end"]) <= 1e-4 * (oa["r_end"] - r0)
+    if oa["accepted"] == ob["accepted"]:
+        d = np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0))))
+        assert d <= 1e-5, d
+
+
+def test_replayed_window_maa_vs_fp64():
+    text = derive("config3_maa.txt", Abins=16, Pbins=8, Ebins=32, R0=15, dr="1e-6")
+    a, b = _pair(text, 3, 1e-6)
+    out = a.evolutionLoop(max_iters=150, log_cap=1000)
+    log = out["log"]
+    rb = np.concatenate([[15.0], log[:-1, 1]])
+    b.replay(rb, log[:, 2])
+    d = np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0))))
+    assert d <= 1e-5, d
+
+
+def test_config1_shape_iteration_vs_fp64():
+    text = derive("config1_ma.txt", R0=50, dr="1e-4")
+    a, b = _pair(text)
+    me64, me32 = a.step(50.0, 1e-4), b.step(50.0, 1e-4)
+    assert abs(me32 - me64) <= 2e-2 * me64
+    a.accept()
+    b.accept()
+    assert np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0)))) <= 1e-7
+
+
+def test_renormalisation_keeps_unit_norm():
+    text = derive("config0_ma.txt", Abins=16, Ebins=32, R0=20, dr="1e-6")
+    b = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= mixed")))
+    assert b.lib.xf_set_option(b.h, b"renorm_every", 1.0) == 0
+    b.evolutionLoop(max_iters=50)
+    psi = b.get_state(0)
+    n = (psi ** 2).sum(axis=1)
+    assert np.max(np.abs(n - 1.0)) < 1e-13
+
+
+def test_device_control_equals_host_loop_mixed():
+    text = derive("config0_ma.txt", Abins=32, Ebins=64).replace("precision= fp64", "precision= mixed")
+    s1 = xg.Simulation(xg.Config.from_text(text))
+    s2 = xg.Simulation(xg.Config.from_text(text))
+    a = s1.evolutionLoop(max_iters=120, log_cap=1000)
+    b = s2.evolutionLoop(max_iters=120, log_cap=1000, device_control=True)
+    assert (a["iterations"], a["accepted"]) == (b["iterations"], b["accepted"])
+    np.testing.assert_array_equal(a["log"], b["log"])
+    assert np.array_equal(s1.get_state(0), s2.get_state(0))
+
+
+def test_mixed_rejects_unkept_buffers():
+    b = xg.Simulation(xg.Config.from_text(derive("config0_ma.txt", Abins=4, Ebins=8, precision="mixed")))
+    with pytest.raises(xg.XflatError):
+        b.get_state(1)

@@ -38,6 +38,10 @@ struct Ctl {
     double* psi4;
     double* S0;
     double* S4;
+    float* m0hi;          // mixed precision: psi0 and candidate as FP32 value + FP32 compensation
+    float* m0lo;
+    float* m4hi;
+    float* m4lo;
     unsigned int ticket[4];  // last-block tickets per phase
     int done;             // device control: no further iterations
     int nan_seen;
@@ -45,6 +49,7 @@ struct Ctl {
     long long accepted;   // counter
     long long max_iters;  // Ts
     long long log_len;    // accepted-step records written to the log
+    int renorm_due;       // mixed precision: the last accepted step calls for a renormalisation
 };
 
 // Kernel parameters (passed by value).
@@ -53,6 +58,8 @@ struct Dev {
     int nbeams, A, P, ne, epad;
     const double* fv;     // [4][epad]
     const double* hvac;   // [2][epad]: h00 part, then h01 real part
+    const float* fvf;     // FP32 copies for the mixed-precision kernels
+    const float* hvf;
     const double* cos2R;  // [A]
     const double* dcos2R; // [A]
     const double* sinR;   // [A]
@@ -74,6 +81,7 @@ struct Dev {
     int has_matter;
     double mat_coeff, nbfar, nb0, hNS;
     int device_control;   // phase C runs the accept/reject/dr controller
+    int renorm_every;     // mixed precision: renormalise psi0 every this many accepted steps
     int debug_psi3;       // phase C also stores U(h4, dl2) psi3 into psi3 (the reference's S10 result)
 };
 

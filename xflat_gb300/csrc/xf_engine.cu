@@ -201,6 +201,12 @@ void xf_handle::release()
     if (st) cudaStreamDestroy(st);
 }
 
+void xf_handle::launch_ph(int phase, const Dev& d)
+{
+    if (mixed) xf::mixed_launch_phase(phase, d, shape, st);
+    else xf::launch_phase(phase, d, shape, st);
+}
+
 int xf_handle::pull_ctl()
 {
     XF_CUDA(this, cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -273,7 +279,6 @@ int xf_handle::refresh_j0(double r)
 
 int xf_handle::step(double r, double dr, double* max_err)
 {
-    if (mixed) return xf::mixed_step(this, mixed, r, dr, max_err);
     int rc;
     if ((rc = push_inputs(r, dr))) return rc;
     Dev d = dev;
@@ -282,11 +287,11 @@ int xf_handle::step(double r, double dr, double* max_err)
     xf::launch_geometry(d, st);
     if ((rc = refresh_j0(r))) return rc;
     if (time_phases) XF_CUDA(this, cudaEventRecord(ev[0], st));
-    xf::launch_phase(xf::PH_A, d, shape, st);
+    launch_ph(xf::PH_A, d);
     if (time_phases) XF_CUDA(this, cudaEventRecord(ev[1], st));
-    xf::launch_phase(xf::PH_B, d, shape, st);
+    launch_ph(xf::PH_B, d);
     if (time_phases) XF_CUDA(this, cudaEventRecord(ev[2], st));
-    xf::launch_phase(xf::PH_C, d, shape, st);
+    launch_ph(xf::PH_C, d);
     if (time_phases) XF_CUDA(this, cudaEventRecord(ev[3], st));
     XF_CUDA(this, cudaGetLastError());
     launches += 4;
@@ -309,15 +314,27 @@ int xf_handle::step(double r, double dr, double* max_err)
 
 int xf_handle::accept()
 {
-    if (mixed) return xf::mixed_accept(this, mixed, last_r + last_dr);
     Dev d = dev;
-    xf::launch_accept(d, st);
+    bool renormed = false;
+    if (mixed) {
+        xf::mixed_launch_accept(d, st);
+        // unitarity renormalisation of the accepted FP32 state every renorm_every steps
+        if (renorm_every > 0 && ++accepts_since_renorm >= renorm_every) {
+            xf::mixed_launch_renorm(d, 0, st);
+            accepts_since_renorm = 0;
+            renormed = true;
+            launches++;
+        }
+    } else {
+        xf::launch_accept(d, st);
+    }
     XF_CUDA(this, cudaGetLastError());
     XF_CUDA(this, cudaStreamSynchronize(st));
     launches++;
     // J0 now holds the candidate's moments at point 2 of the last step, which
-    // is point 0 of radius r + dr.
-    j0_valid = true;
+    // is point 0 of radius r + dr; after a renormalisation it is recomputed
+    // from the renormalised state at the next step.
+    j0_valid = !renormed;
     j0_r = last_r + last_dr;
     return XF_OK;
 }
@@ -388,6 +405,7 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
     d.device_control = 1;
     d.log = d_log;
     d.log_cap = log_cap_dev;
+    d.renorm_every = mixed ? renorm_every : 0;
     if (timed) {
         const size_t need = (size_t)k * 6;
         while (tev.size() < need) {
@@ -400,9 +418,15 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
     XF_CUDA(this, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < k; ++i) {
         xf::launch_geometry(d, st);
+        if (mixed) {
+            // after a flagged accepted step: renormalise psi0, refresh its exact
+            // sums and its moments at stage point 0 of the new radius
+            xf::mixed_launch_renorm(d, 1, st);
+            xf::launch_moments(d, nullptr, 0, &d_ctl->J0[0], st, 1);
+        }
         for (int ph = 0; ph < 3; ++ph) {
             if (timed) cudaEventRecordWithFlags(tev[6 * i + 2 * ph], st, cudaEventRecordExternal);
-            xf::launch_phase(ph, d, shape, st);
+            launch_ph(ph, d);
             if (timed) cudaEventRecordWithFlags(tev[6 * i + 2 * ph + 1], st, cudaEventRecordExternal);
         }
     }
@@ -420,7 +444,6 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
 
 int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
 {
-    if (mixed) return xf::mixed_run_device(this, mixed, o, s);
     double r = std::isnan(o.r0) ? cfg.R0 : o.r0;
     double dr = std::isnan(o.dr0) ? cfg.dr : o.dr0;
     const long Ts = o.max_iters >= 0 ? o.max_iters : cfg.Ts;
@@ -454,6 +477,12 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     h_ctl->done = (r < cfg.Rn && Ts > 0) ? 0 : 1;
     for (int i = 0; i < 4; ++i) h_ctl->ticket[i] = 0;
     XF_CUDA(this, cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    // instantiate the graph sizes this run needs before the timed region starts
+    {
+        cudaGraphExec_t ex;
+        if (Ts > 0 && (rc = get_graph((int)std::min<long>(k, Ts), o.time_phases != 0, &ex))) return rc;
+        if (Ts > k && Ts % k && (rc = get_graph((int)(Ts % k), o.time_phases != 0, &ex))) return rc;
+    }
     const double t0 = now_s();
     XF_CUDA(this, cudaEventRecord(ev[4], st));
     long long prev_iters = 0;
@@ -578,6 +607,9 @@ int xf_set_option(xf_handle* h, const char* name, double value)
     const std::string n = name;
     if (n == "debug_psi3") {
         h->debug_psi3 = value != 0.;
+    } else if (n == "renorm_every") {
+        if (value < 0.) return h->fail(XF_EINVAL, "renorm_every must be >= 0");
+        h->renorm_every = (int)value;
     } else if (n == "threads") {
         const int t = (int)value;
         if (t != 0 && (t < 32 || t > 256 || t % 32)) return h->fail(XF_EINVAL, "threads must be a multiple of 32 in [32, 256]");
@@ -658,7 +690,7 @@ int xf_angle_bins(xf_handle* h, double r, double dr, double* cosb, double* sinb,
 int xf_calc_hvv(xf_handle* h, int which, int pt, double r, double dr, double* hvv)
 {
     if (!h || !hvv || pt < 0 || pt > 2) return XF_EINVAL;
-    if (h->mixed) return h->fail(XF_EUNSUPPORTED, "xf_calc_hvv is available for the FP64 path");
+    if (h->mixed && which != 0) return h->fail(XF_EUNSUPPORTED, "the mixed path keeps only psi0's energy sums");
     int rc;
     if ((rc = h->pull_ctl())) return rc;
     if ((rc = h->push_inputs(r, dr))) return rc;

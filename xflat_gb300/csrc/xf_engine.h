@@ -52,6 +52,8 @@ struct xf_handle {
     double j0_r = 0.;
     double last_r = 0., last_dr = 0.;
     int debug_psi3 = 0;
+    int renorm_every = 16;        // mixed precision: accepted steps between renormalisations
+    int accepts_since_renorm = 0;
     int time_phases = 0;
     double phase_ms[3] = {0., 0., 0.};
     long phase_n[3] = {0, 0, 0};
@@ -70,6 +72,7 @@ struct xf_handle {
     int init(const xf_config& c);
     void release();
     int pull_ctl();
+    void launch_ph(int phase, const xf::Dev& d);
     int set_state(const double* psi);
     int get_state(int which, double* psi);
     int push_inputs(double r, double dr);

@@ -18,7 +18,7 @@ Shape default_shape(int nbeams, int epad);
 
 void launch_geometry(const Dev& d, cudaStream_t st);
 void launch_esum(const Dev& d, const double* psi, double* S, cudaStream_t st);
-void launch_moments(const Dev& d, const double* S, int pt, double* Jout, cudaStream_t st);
+void launch_moments(const Dev& d, const double* S, int pt, double* Jout, cudaStream_t st, int conditional = 0);
 void launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st);
 void launch_accept(const Dev& d, cudaStream_t st);
 void launch_hvv_eval(const Dev& d, const double* J, int pt, double* hvv, cudaStream_t st);

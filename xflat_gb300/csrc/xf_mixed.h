@@ -1,6 +1,11 @@
-// Mixed-precision path (xf_mixed.cu): FP32 beam state and SU(2) rotations with
-// FP64 moment reduction, error estimate, step control and renormalisation.
+// Mixed-precision path (xf_mixed.cu): FP32 beam state (value + compensation)
+// and SU(2) rotations with FP64 moment reduction, error reduction, step
+// control and renormalisation.
 #pragma once
+#include <cuda_runtime.h>
+
+#include "xf_device.cuh"
+#include "xf_kernels.h"
 #include "xflat_gpu.h"
 
 struct xf_handle;
@@ -11,7 +16,9 @@ Mixed* mixed_create(xf_handle* h);
 void mixed_destroy(Mixed* m);
 int mixed_set_state(xf_handle* h, Mixed* m, const double* psi);
 int mixed_get_state(xf_handle* h, Mixed* m, int which, double* psi);
-int mixed_step(xf_handle* h, Mixed* m, double r, double dr, double* max_err);
-int mixed_accept(xf_handle* h, Mixed* m, double r_new);
-int mixed_run_device(xf_handle* h, Mixed* m, const xf_run_opts& o, xf_run_stats& s);
+void mixed_launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st);
+void mixed_launch_accept(const Dev& d, cudaStream_t st);
+// Renormalises psi0 and recomputes its exact FP64 energy sums; with
+// `conditional` only when the step controller flagged it.
+void mixed_launch_renorm(const Dev& d, int conditional, cudaStream_t st);
 }  // namespace xf
