@@ -226,6 +226,9 @@ int xf_batch_get_state(xf_batch* b, int inst, double* psi);
 /* Advance every unfinished instance by up to max_iters iterations (< 0: each
  * instance's Ts); per-instance results in iters/accepted/r_end (may be NULL). */
 int xf_batch_run(xf_batch* b, long max_iters, long* iters, long* accepted, double* r_end, double* seconds);
+/* Beams per tile chosen by the autotuner at creation, and the measured time
+ * (ms, 8 iterations) of each candidate tile shape {2, 4, 8} (may be NULL). */
+int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms);
 
 #ifdef __cplusplus
 }

@@ -290,6 +290,12 @@ class Batch:
         self._c(self.lib.xf_batch_get_state(self.h, i, _dp(out)), "xf_batch_get_state")
         return out.reshape(nb, 4, ne)
 
+    def tile_shape(self):
+        w = ctypes.c_int()
+        ms = np.zeros(3)
+        self._c(self.lib.xf_batch_tile_shape(self.h, ctypes.byref(w), _dp(ms)), "xf_batch_tile_shape")
+        return w.value, ms
+
     def run(self, max_iters=-1):
         n = len(self.cfgs)
         it = (ctypes.c_long * n)()

@@ -1,16 +1,433 @@
-// Batched path: placeholder until the batched kernels land.
+// Batched path: many independent MA simulations of uneven angle and energy
+// counts, each with its own adaptive step control, advanced together.
+//
+// Every instance keeps its own tables, state, control block and partial-sum
+// buffer (an xf_handle).  One iteration of the batch is one launch per stage
+// kernel over a work list of tiles: a tile is `warps` consecutive beams of one
+// instance, one warp per beam.  The blocks of an instance form that instance's
+// reduction group: the last of its tiles to finish reduces the instance's
+// moments in fixed order and, in the last phase, runs the instance's step
+// controller (accept/reject, dr, termination; src/Nmr.cpp:227-249).  An
+// instance that has finished skips its tiles, so instances with different step
+// counts share the launches.  Iterations are captured in CUDA graphs and the
+// host only polls a compact status array between graph launches.  The tile
+// shape (warps per tile) is chosen at creation by timing the candidates on the
+// batch itself (xf_batch_create's autotuner).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "xf_common.cuh"
+#include "xf_engine.h"
+#include "xf_fp64.cuh"
+#include "xf_mixed.cuh"
 #include "xflat_gpu.h"
 
-extern "C" {
-int xf_batch_create(const xf_config*, int, xf_batch** out)
+using xf::Ctl;
+using xf::Dev;
+
+namespace {
+
+using namespace xf::detail;
+
+struct Tile {
+    int inst, first, idx, count;  // instance, first beam, tile index and tile count within the instance
+};
+
+struct Status {
+    double r, dr;
+    long long iters, accepted;
+    int done, nan_seen;
+};
+
+__device__ __forceinline__ RedTarget tile_target(const Dev& d, const Tile& t, int phase)
 {
-    if (out) *out = nullptr;
-    return XF_EUNSUPPORTED;
+    RedTarget rt;
+    rt.partials = d.partials;
+    rt.idx = t.idx;
+    rt.count = t.count;
+    rt.ticket = &d.ctl->ticket[phase];
+    return rt;
 }
-int xf_batch_destroy(xf_batch*) { return XF_OK; }
-const char* xf_batch_last_error(const xf_batch*) { return "batched path not available in this build"; }
-int xf_batch_dims(const xf_batch*, int, int*, int*) { return XF_EUNSUPPORTED; }
-int xf_batch_set_state(xf_batch*, int, const double*) { return XF_EUNSUPPORTED; }
-int xf_batch_get_state(xf_batch*, int, double*) { return XF_EUNSUPPORTED; }
-int xf_batch_run(xf_batch*, long, long*, long*, double*, double*) { return XF_EUNSUPPORTED; }
+
+__global__ void k_batch_geometry(const Dev* __restrict__ devs, const int2* __restrict__ angles, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 a = angles[i];
+    geometry_body(devs[a.x], a.y);
 }
+
+template <int PREC, int PH>
+__global__ void __launch_bounds__(256) k_batch_phase(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
+{
+    const Tile t = tiles[blockIdx.x];
+    const Dev& d = devs[t.inst];
+    const RedTarget rt = tile_target(d, t, PH);
+    if (PREC == 0) {
+        if (PH == xf::PH_A) xf::fp64::phaseA_body<0>(d, t.first, d.nbeams, rt);
+        else if (PH == xf::PH_B) xf::fp64::phaseB_body<0>(d, t.first, d.nbeams, rt);
+        else xf::fp64::phaseC_body<0>(d, t.first, d.nbeams, rt);
+    } else {
+        if (PH == xf::PH_A) xf::mixed::phaseA_body<0>(d, t.first, d.nbeams, rt);
+        else if (PH == xf::PH_B) xf::mixed::phaseB_body<0>(d, t.first, d.nbeams, rt);
+        else xf::mixed::phaseC_body<0>(d, t.first, d.nbeams, rt);
+    }
+}
+
+// Mixed precision: flagged renormalisation with exact energy sums (warp tiles)
+// and the refreshed moments of psi0 (thread tiles of 256 beams).
+__global__ void __launch_bounds__(256) k_batch_renorm(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
+{
+    const Tile t = tiles[blockIdx.x];
+    xf::mixed::esum_body(devs[t.inst], t.first, devs[t.inst].nbeams, 1, 1);
+}
+
+__global__ void __launch_bounds__(256) k_batch_moments(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
+{
+    const Tile t = tiles[blockIdx.x];
+    const Dev& d = devs[t.inst];
+    moments_body<0>(d, t.first, d.nbeams, tile_target(d, t, xf::PH_MOM), nullptr, 0, &d.ctl->J0[0], 1);
+}
+
+__global__ void k_batch_status(const Dev* __restrict__ devs, int n, Status* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Ctl* c = devs[i].ctl;
+    Status s;
+    s.r = c->r;
+    s.dr = c->dr;
+    s.iters = c->iters;
+    s.accepted = c->accepted;
+    s.done = c->done;
+    s.nan_seen = c->nan_seen;
+    out[i] = s;
+}
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct xf_batch {
+    std::vector<xf_handle*> h;
+    int prec = XF_PREC_FP64;
+    int warps = 8;                  // beams per tile (= warps per block)
+    cudaStream_t st = nullptr;
+    Dev* d_devs = nullptr;
+    Tile* d_wtiles = nullptr;       // warp tiles for the stage kernels
+    Tile* d_ttiles = nullptr;       // thread tiles for the moment kernel
+    int2* d_angles = nullptr;
+    double* d_part = nullptr;       // partial sums of every instance
+    Status* d_status = nullptr;
+    Status* h_status = nullptr;     // pinned
+    int nwt = 0, ntt = 0, nang = 0;
+    struct G {
+        int k;
+        cudaGraphExec_t ex;
+    };
+    std::vector<G> graphs;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    double tuned_ms[3] = {0., 0., 0.};
+    std::string err;
+
+    int fail(int code, const std::string& m)
+    {
+        err = m;
+        return code;
+    }
+};
+
+#define XB_CUDA(b, call)                                                                             \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return (b)->fail(XF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+void drop_graphs(xf_batch* b)
+{
+    for (auto& g : b->graphs)
+        if (g.ex) cudaGraphExecDestroy(g.ex);
+    b->graphs.clear();
+}
+
+// Work lists and per-instance device parameter blocks for a tile shape.
+int build_lists(xf_batch* b, int warps)
+{
+    drop_graphs(b);
+    b->warps = warps;
+    const int n = (int)b->h.size();
+    std::vector<Tile> wt, tt;
+    std::vector<int2> ang;
+    std::vector<Dev> devs(n);
+    std::vector<size_t> part_off(n);
+    size_t part_total = 0;
+    for (int i = 0; i < n; ++i) {
+        const xf_handle* h = b->h[i];
+        const int nwti = (h->nbeams + warps - 1) / warps;
+        const int ntti = (h->nbeams + 255) / 256;
+        for (int t = 0; t < nwti; ++t) wt.push_back(Tile{i, t * warps, t, nwti});
+        for (int t = 0; t < ntti; ++t) tt.push_back(Tile{i, t * 256, t, ntti});
+        for (int a = 0; a < h->A; ++a) ang.push_back(make_int2(i, a));
+        part_off[i] = part_total;
+        part_total += (size_t)std::max(nwti, ntti) * xf::kPartStride;
+    }
+    if (b->d_part) cudaFree(b->d_part);
+    if (b->d_wtiles) cudaFree(b->d_wtiles);
+    if (b->d_ttiles) cudaFree(b->d_ttiles);
+    if (b->d_angles) cudaFree(b->d_angles);
+    if (b->d_devs) cudaFree(b->d_devs);
+    b->d_part = nullptr;
+    b->d_wtiles = b->d_ttiles = nullptr;
+    b->d_angles = nullptr;
+    b->d_devs = nullptr;
+    XB_CUDA(b, cudaMalloc(&b->d_part, part_total * sizeof(double)));
+    XB_CUDA(b, cudaMemset(b->d_part, 0, part_total * sizeof(double)));
+    for (int i = 0; i < n; ++i) {
+        devs[i] = b->h[i]->dev;
+        devs[i].device_control = 1;
+        devs[i].log = nullptr;
+        devs[i].log_cap = 0;
+        devs[i].renorm_every = b->prec == XF_PREC_MIXED ? b->h[i]->renorm_every : 0;
+        devs[i].partials = b->d_part + part_off[i];
+    }
+    XB_CUDA(b, cudaMalloc(&b->d_devs, n * sizeof(Dev)));
+    XB_CUDA(b, cudaMemcpy(b->d_devs, devs.data(), n * sizeof(Dev), cudaMemcpyHostToDevice));
+    XB_CUDA(b, cudaMalloc(&b->d_wtiles, wt.size() * sizeof(Tile)));
+    XB_CUDA(b, cudaMemcpy(b->d_wtiles, wt.data(), wt.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    XB_CUDA(b, cudaMalloc(&b->d_ttiles, tt.size() * sizeof(Tile)));
+    XB_CUDA(b, cudaMemcpy(b->d_ttiles, tt.data(), tt.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    XB_CUDA(b, cudaMalloc(&b->d_angles, ang.size() * sizeof(int2)));
+    XB_CUDA(b, cudaMemcpy(b->d_angles, ang.data(), ang.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    b->nwt = (int)wt.size();
+    b->ntt = (int)tt.size();
+    b->nang = (int)ang.size();
+    return XF_OK;
+}
+
+void launch_iteration(xf_batch* b)
+{
+    const int threads = 32 * b->warps;
+    k_batch_geometry<<<(b->nang + 127) / 128, 128, 0, b->st>>>(b->d_devs, b->d_angles, b->nang);
+    if (b->prec == XF_PREC_MIXED) {
+        k_batch_renorm<<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        k_batch_moments<<<b->ntt, 256, 0, b->st>>>(b->d_devs, b->d_ttiles);
+        k_batch_phase<1, xf::PH_A><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        k_batch_phase<1, xf::PH_B><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        k_batch_phase<1, xf::PH_C><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+    } else {
+        k_batch_phase<0, xf::PH_A><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        k_batch_phase<0, xf::PH_B><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        k_batch_phase<0, xf::PH_C><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+    }
+}
+
+int get_graph(xf_batch* b, int k, cudaGraphExec_t* out)
+{
+    for (auto& g : b->graphs)
+        if (g.k == k) {
+            *out = g.ex;
+            return XF_OK;
+        }
+    cudaGraph_t g;
+    XB_CUDA(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < k; ++i) launch_iteration(b);
+    const int n = (int)b->h.size();
+    k_batch_status<<<(n + 63) / 64, 64, 0, b->st>>>(b->d_devs, n, b->d_status);
+    cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(Status), cudaMemcpyDeviceToHost, b->st);
+    cudaError_t ce = cudaStreamEndCapture(b->st, &g);
+    if (ce != cudaSuccess) return b->fail(XF_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    cudaGraphExec_t ex;
+    ce = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return b->fail(XF_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+    b->graphs.push_back(xf_batch::G{k, ex});
+    *out = ex;
+    return XF_OK;
+}
+
+// Device-controlled run of every instance from its config's R0/dr (or from
+// where a previous run stopped when `resume`), max_iters iterations each.
+int run(xf_batch* b, long max_iters, bool resume, double* device_ms)
+{
+    const int n = (int)b->h.size();
+    long budget = max_iters;
+    for (int i = 0; i < n; ++i) {
+        xf_handle* h = b->h[i];
+        const long Ts = max_iters >= 0 ? max_iters : h->cfg.Ts;
+        budget = std::max(budget, Ts);
+        double r = h->cfg.R0, dr = h->cfg.dr;
+        if (resume) {
+            r = b->h_status[i].r;
+            dr = b->h_status[i].dr;
+        }
+        int rc = h->start_device_run(r, dr, Ts);
+        if (rc) return b->fail(rc, "instance " + std::to_string(i) + ": " + h->err);
+    }
+    const int k = 8;
+    cudaGraphExec_t ex;
+    int rc;
+    if ((rc = get_graph(b, k, &ex))) return rc;
+    XB_CUDA(b, cudaEventRecord(b->e0, b->st));
+    long done_iters = 0;
+    while (true) {
+        XB_CUDA(b, cudaGraphLaunch(ex, b->st));
+        XB_CUDA(b, cudaStreamSynchronize(b->st));
+        done_iters += k;
+        bool all = true;
+        for (int i = 0; i < n; ++i) all = all && b->h_status[i].done;
+        if (all || done_iters >= budget + k) break;
+    }
+    XB_CUDA(b, cudaEventRecord(b->e1, b->st));
+    XB_CUDA(b, cudaEventSynchronize(b->e1));
+    float ms = 0.f;
+    XB_CUDA(b, cudaEventElapsedTime(&ms, b->e0, b->e1));
+    if (device_ms) *device_ms = ms;
+    // hand the control blocks back to host-driven use
+    for (int i = 0; i < n; ++i) {
+        xf_handle* h = b->h[i];
+        XB_CUDA(b, cudaMemsetAsync(&h->d_ctl->done, 0, sizeof(int), b->st));
+        h->j0_valid = true;
+        h->j0_r = b->h_status[i].r;
+    }
+    XB_CUDA(b, cudaStreamSynchronize(b->st));
+    for (int i = 0; i < n; ++i)
+        if (b->h_status[i].nan_seen) return b->fail(XF_ENAN, "instance " + std::to_string(i) + ": step error is NaN");
+    return XF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out)
+{
+    if (!cfgs || n <= 0 || !out) return XF_EINVAL;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i)
+        if (cfgs[i].geometry != XF_GEOM_MA || cfgs[i].precision != cfgs[0].precision) return XF_EUNSUPPORTED;
+    xf_batch* b = new xf_batch();
+    b->prec = cfgs[0].precision;
+    int rc = XF_OK;
+    for (int i = 0; i < n && rc == XF_OK; ++i) {
+        xf_handle* h = nullptr;
+        rc = xf_create(&cfgs[i], &h);
+        if (rc == XF_OK) b->h.push_back(h);
+    }
+    if (rc == XF_OK && cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) rc = XF_ECUDA;
+    if (rc == XF_OK && (cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess)) rc = XF_ECUDA;
+    if (rc == XF_OK && cudaMalloc(&b->d_status, n * sizeof(Status)) != cudaSuccess) rc = XF_ENOMEM;
+    if (rc == XF_OK && cudaMallocHost(&b->h_status, n * sizeof(Status)) != cudaSuccess) rc = XF_ENOMEM;
+    // autotune the tile shape on the batch itself: a few iterations per
+    // candidate from the initial states, which are restored afterwards
+    if (rc == XF_OK) {
+        const int cand[3] = {2, 4, 8};
+        double best = 1e300;
+        int best_w = 8;
+        for (int c = 0; c < 3 && rc == XF_OK; ++c) {
+            rc = build_lists(b, cand[c]);
+            double ms = 0.;
+            if (rc == XF_OK) rc = run(b, 2, false, nullptr);      // first launch instantiates the graph
+            if (rc == XF_OK) rc = run(b, 8, false, &ms);
+            b->tuned_ms[c] = ms;
+            if (rc == XF_OK && ms < best) {
+                best = ms;
+                best_w = cand[c];
+            }
+        }
+        if (rc == XF_OK) rc = build_lists(b, best_w);
+        for (int i = 0; i < n && rc == XF_OK; ++i) {
+            std::vector<double> psi;
+            xf::initial_state(b->h[i]->nbeams, b->h[i]->ne, cfgs[i].seed, cfgs[i].noise_amp, psi);
+            rc = b->h[i]->set_state(psi.data());
+        }
+    }
+    if (rc != XF_OK) {
+        xf_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return XF_OK;
+}
+
+int xf_batch_destroy(xf_batch* b)
+{
+    if (!b) return XF_EINVAL;
+    drop_graphs(b);
+    for (auto* h : b->h) xf_destroy(h);
+    if (b->d_devs) cudaFree(b->d_devs);
+    if (b->d_wtiles) cudaFree(b->d_wtiles);
+    if (b->d_ttiles) cudaFree(b->d_ttiles);
+    if (b->d_angles) cudaFree(b->d_angles);
+    if (b->d_part) cudaFree(b->d_part);
+    if (b->d_status) cudaFree(b->d_status);
+    if (b->h_status) cudaFreeHost(b->h_status);
+    if (b->e0) cudaEventDestroy(b->e0);
+    if (b->e1) cudaEventDestroy(b->e1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return XF_OK;
+}
+
+const char* xf_batch_last_error(const xf_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int xf_batch_dims(const xf_batch* b, int inst, int* nbeams, int* ebins)
+{
+    if (!b || inst < 0 || inst >= (int)b->h.size()) return XF_EINVAL;
+    if (nbeams) *nbeams = b->h[inst]->nbeams;
+    if (ebins) *ebins = b->h[inst]->ne;
+    return XF_OK;
+}
+
+int xf_batch_set_state(xf_batch* b, int inst, const double* psi)
+{
+    if (!b || !psi || inst < 0 || inst >= (int)b->h.size()) return XF_EINVAL;
+    const int rc = b->h[inst]->set_state(psi);
+    if (rc) b->err = b->h[inst]->err;
+    return rc;
+}
+
+int xf_batch_get_state(xf_batch* b, int inst, double* psi)
+{
+    if (!b || !psi || inst < 0 || inst >= (int)b->h.size()) return XF_EINVAL;
+    const int rc = b->h[inst]->get_state(0, psi);
+    if (rc) b->err = b->h[inst]->err;
+    return rc;
+}
+
+int xf_batch_run(xf_batch* b, long max_iters, long* iters, long* accepted, double* r_end, double* seconds)
+{
+    if (!b) return XF_EINVAL;
+    const double t0 = now_s();
+    double ms = 0.;
+    const int rc = run(b, max_iters, false, &ms);
+    const int n = (int)b->h.size();
+    for (int i = 0; i < n; ++i) {
+        if (iters) iters[i] = (long)b->h_status[i].iters;
+        if (accepted) accepted[i] = (long)b->h_status[i].accepted;
+        if (r_end) r_end[i] = b->h_status[i].r;
+    }
+    if (seconds) *seconds = ms > 0. ? ms * 1e-3 : now_s() - t0;
+    return rc;
+}
+
+int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms)
+{
+    if (!b) return XF_EINVAL;
+    if (warps) *warps = b->warps;
+    if (tuned_ms)
+        for (int i = 0; i < 3; ++i) tuned_ms[i] = b->tuned_ms[i];
+    return XF_OK;
+}
+
+}  // extern "C"

@@ -134,13 +134,23 @@ __device__ __forceinline__ void add_moment(const Dev& d, double val, int z, int 
 __device__ __forceinline__ int comp_of(int k) { return k == 0 ? 0 : (k == 1 ? 2 : 3); }
 
 // Block-level combination of per-lane moment accumulators followed by the
-// last-block reduction over blocks.  Lanes l with l % G == 0 (G = 32/NV) own
+// last-block reduction over the group's blocks.  Lanes l with l % G == 0 (G = 32/NV) own
 // value v = l / G; values v < nused feed moments.  Returns true in the last
 // block, with s_out[0..nused*K) holding the grid totals and s_out[31] the grid
 // maximum of `mx` (ignored unless with_max).
+// Where a group of blocks reduces its per-block partials: the block's slot
+// `idx` of `count` slots at `partials`, and the ticket that elects the last
+// block of the group (single simulation: the grid; batch: one instance's tiles).
+struct RedTarget {
+    double* partials;
+    int idx;
+    int count;
+    unsigned int* ticket;
+};
+
 template <int K>
-__device__ inline bool block_and_grid_reduce(const Dev& d, int phase, int G, int nused, const double (&acc)[K], double mx,
-                                      bool with_max, double* s_warp, double* s_out)
+__device__ inline bool group_reduce(const RedTarget& rt, int G, int nused, const double (&acc)[K], double mx,
+                                    bool with_max, double* s_warp, double* s_out)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nout = nused * K;
@@ -151,7 +161,7 @@ __device__ inline bool block_and_grid_reduce(const Dev& d, int phase, int G, int
     }
     if (with_max && lane == 0) s_warp[warp * 32 + 31] = mx;
     __syncthreads();
-    double* part = d.partials + (size_t)blockIdx.x * kPartStride;
+    double* part = rt.partials + (size_t)rt.idx * kPartStride;
     if ((int)threadIdx.x < nout) {
         double t = 0.;
         for (int w = 0; w < nw; ++w) t += s_warp[w * 32 + threadIdx.x];
@@ -166,8 +176,8 @@ __device__ inline bool block_and_grid_reduce(const Dev& d, int phase, int G, int
     __syncthreads();
     __shared__ int s_last;
     if (threadIdx.x == 0) {
-        const unsigned t = atomicAdd(&d.ctl->ticket[phase], 1u);
-        s_last = (t == gridDim.x - 1);
+        const unsigned t = atomicAdd(rt.ticket, 1u);
+        s_last = (t == (unsigned)rt.count - 1);
     }
     __syncthreads();
     if (!s_last) return false;
@@ -178,8 +188,8 @@ __device__ inline bool block_and_grid_reduce(const Dev& d, int phase, int G, int
 #pragma unroll
     for (int k = 0; k < 32; ++k) vals[k] = 0.;
     double m = -1.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-        const double* pb = d.partials + (size_t)b * kPartStride;
+    for (int b = threadIdx.x; b < rt.count; b += blockDim.x) {
+        const double* pb = rt.partials + (size_t)b * kPartStride;
 #pragma unroll
         for (int k = 0; k < 31; ++k)
             if (k < nout) vals[k] += __ldcg(pb + k);
@@ -208,7 +218,7 @@ __device__ inline bool block_and_grid_reduce(const Dev& d, int phase, int G, int
             s_out[31] = mm;
         }
     }
-    if (threadIdx.x == 0) d.ctl->ticket[phase] = 0u;
+    if (threadIdx.x == 0) *rt.ticket = 0u;
     __syncthreads();
     return true;
 }
@@ -251,6 +261,130 @@ __device__ inline bool step_control(const Dev& d, Ctl* ctl, double me)
     ctl->renorm_due = (acc && d.renorm_every > 0 && ctl->accepted % d.renorm_every == 0) ? 1 : 0;
     if (!(r < d.Rn) || ctl->iters >= ctl->max_iters || ctl->nan_seen) ctl->done = 1;
     return acc;
+}
+
+}  // namespace detail
+}  // namespace xf
+
+namespace xf {
+namespace detail {
+// The whole grid as one reduction group (single simulation).
+__device__ __forceinline__ RedTarget grid_target(const Dev& d, int phase)
+{
+    RedTarget rt;
+    rt.partials = d.partials;
+    rt.idx = blockIdx.x;
+    rt.count = gridDim.x;
+    rt.ticket = &d.ctl->ticket[phase];
+    return rt;
+}
+}  // namespace detail
+}  // namespace xf
+
+namespace xf {
+namespace detail {
+
+// phy::calcAngleBins at r, r+dr/2, r+dr and phy::calcDeltaLs for the three
+// path segments (src/Nmr.cpp:153-173, src/Phy_MA.cpp:172-227,
+// src/Phy_MAA.cpp:194-241) for angle bin `ang`.  Under device control angle 0
+// also evaluates the matter term at the three points (src/Matt.cpp:31-64).
+__device__ inline void geometry_body(const Dev& d, int ang)
+{
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    const double r = ctl->r, dr = ctl->dr;
+    const double dr2 = .5 * dr;
+    const double rdr = r + dr;
+    const double rdr2 = r + dr2;
+    const double rp[3] = {r, rdr2, rdr};
+    if (d.device_control && ang == 0) {
+#pragma unroll
+        for (int pt = 0; pt < 3; ++pt) {
+            double hm = 0.;
+            if (d.has_matter) {
+                const double R = 10. / rp[pt];
+                const double far = d.nbfar * (R * R * R);
+                const double near = d.nb0 * exp((d.Rv - rp[pt]) / d.hNS);
+                hm = d.mat_coeff * (far + near) * .5;
+            }
+            ctl->hm[pt] = hm;
+        }
+    }
+    if (ang >= d.A) return;
+    double c[3];
+#pragma unroll
+    for (int pt = 0; pt < 3; ++pt) {
+        const double ra = d.Rv / rp[pt];
+        const double r2 = ra * ra;
+        c[pt] = sqrt(1. - r2 * (1. - d.cos2R[ang]));
+        d.geo[geo_idx(0, pt, ang, d.A)] = c[pt];
+        d.geo[geo_idx(1, pt, ang, d.A)] = ra * d.sinR[ang];
+        d.geo[geo_idx(2, pt, ang, d.A)] = .5 * (1. / c[pt]) * r2 * d.dcos2R[ang];
+    }
+    if (d.geom == 0) {
+        d.geo[geo_idx(3, 0, ang, d.A)] = dr2 / (c[0]);
+        d.geo[geo_idx(3, 1, ang, d.A)] = dr / (c[0]);
+        d.geo[geo_idx(3, 2, ang, d.A)] = dr2 / (c[1]);
+    } else {
+        d.geo[geo_idx(3, 0, ang, d.A)] = dr2 / ((c[0] + c[1]) * .5);
+        d.geo[geo_idx(3, 1, ang, d.A)] = dr / ((c[0] + c[2]) * .5);
+        d.geo[geo_idx(3, 2, ang, d.A)] = dr2 / ((c[1] + c[2]) * .5);
+    }
+}
+
+// Angular moments from per-beam energy sums at stage point pt: the reduction of
+// phy::getHvv_partial (src/Phy_MA.cpp:388-446, src/Phy_MAA.cpp:468-562); one
+// thread per beam over beams first + threadIdx.x, + stride, ...
+template <int GEOM>
+__device__ inline void moments_body(const Dev& d, int first, int stride, const RedTarget& rt,
+                                    const double* __restrict__ Sarg, int pt, double* Jout, int conditional)
+{
+    constexpr int K = NK<GEOM>::K;
+    // conditional: only after a renormalisation flagged by the step controller
+    // (the mixed path refreshes J0 from the renormalised state); the last block
+    // clears the flag once every block has passed this check.
+    if (conditional && !d.ctl->renorm_due) return;
+    const double* __restrict__ S = Sarg ? Sarg : d.ctl->S0;  // null: the cached sums of psi0
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    // lane owns beams gtid, gtid + nthreads, ...; every lane accumulates all 3*K slots
+    double acc3[3][K];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc3[i][k] = 0.;
+    for (int b = first + threadIdx.x; b < d.nbeams; b += stride) {
+        const BeamIdx bi = decode_beam(d, b);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) add_moment<GEOM>(d, S[(size_t)b * 4 + comp_of(i)], comp_of(i), pt, bi, acc3[i]);
+    }
+    // reduce 3*K values over the warp: lane l ends with slot l / (32/16)
+    double v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = 0.;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[i * K + k] = acc3[i][k];
+    const int lane = threadIdx.x & 31;
+    warp_reduce_scatter<16>(v, lane);
+    // slot s = lane/2 = i*K + k; present as a K-vector per slot i via the generic reducer
+    double one[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) one[k] = 0.;
+    // lanes with (lane % 2 == 0) own slot lane/2; re-pack as value v=i (<3) with K moments
+    // by having lane 2*(i*K) gather its K neighbours' slots.
+#pragma unroll
+    for (int k = 0; k < K; ++k) one[k] = __shfl_sync(kFull, v[0], (lane & ~((2 * K) - 1)) + 2 * k);
+    // group leaders are lanes 2*K*i, i.e. G = 2K lanes per value
+    if (!group_reduce<K>(rt, 2 * K, 3, one, 0., false, s_warp, s_out)) return;
+    if (threadIdx.x < kNJ) Jout[threadIdx.x] = 0.;
+    __syncthreads();
+    if ((int)threadIdx.x < 3 * K) {
+        const int i = threadIdx.x / K, k = threadIdx.x % K;
+        Jout[k * 4 + comp_of(i)] = s_out[threadIdx.x];
+    }
+    if (conditional && threadIdx.x == 0) d.ctl->renorm_due = 0;
 }
 
 }  // namespace detail

@@ -442,6 +442,34 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
     return XF_OK;
 }
 
+// Prepares the control block for a device-controlled loop from (r, dr) with
+// an iteration budget Ts: moments of psi0 at stage point 0 of r, counters
+// reset, done set if there is nothing to do.  Synchronous.
+int xf_handle::start_device_run(double r, double dr, long Ts)
+{
+    int rc;
+    if ((rc = push_inputs(r, dr))) return rc;
+    {
+        Dev d = dev;
+        xf::launch_geometry(d, st);
+        if ((rc = refresh_j0(r))) return rc;
+    }
+    if ((rc = pull_ctl())) return rc;
+    h_ctl->r = r;
+    h_ctl->dr = dr;
+    h_ctl->iters = 0;
+    h_ctl->accepted = 0;
+    h_ctl->max_iters = Ts;
+    h_ctl->nan_seen = 0;
+    h_ctl->log_len = 0;
+    h_ctl->renorm_due = 0;
+    h_ctl->done = (r < cfg.Rn && Ts > 0) ? 0 : 1;
+    for (int i = 0; i < 4; ++i) h_ctl->ticket[i] = 0;
+    XF_CUDA(this, cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    XF_CUDA(this, cudaStreamSynchronize(st));
+    return XF_OK;
+}
+
 int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
 {
     double r = std::isnan(o.r0) ? cfg.R0 : o.r0;
@@ -459,24 +487,7 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         if ((rc = dalloc(this, &d_log, 3 * (size_t)o.log_cap))) return rc;
         log_cap_dev = o.log_cap;
     }
-    // moments of psi0 at r (stage point 0), then the control block
-    if ((rc = push_inputs(r, dr))) return rc;
-    {
-        Dev d = dev;
-        xf::launch_geometry(d, st);
-        if ((rc = refresh_j0(r))) return rc;
-    }
-    if ((rc = pull_ctl())) return rc;
-    h_ctl->r = r;
-    h_ctl->dr = dr;
-    h_ctl->iters = 0;
-    h_ctl->accepted = 0;
-    h_ctl->max_iters = Ts;
-    h_ctl->nan_seen = 0;
-    h_ctl->log_len = 0;
-    h_ctl->done = (r < cfg.Rn && Ts > 0) ? 0 : 1;
-    for (int i = 0; i < 4; ++i) h_ctl->ticket[i] = 0;
-    XF_CUDA(this, cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    if ((rc = start_device_run(r, dr, Ts))) return rc;
     // instantiate the graph sizes this run needs before the timed region starts
     {
         cudaGraphExec_t ex;

@@ -81,6 +81,7 @@ struct xf_handle {
     int accept();
     int run_host(const xf_run_opts& o, xf_step_cb cb, void* user, xf_run_stats& s);
     int run_device(const xf_run_opts& o, xf_run_stats& s);
+    int start_device_run(double r, double dr, long Ts);
     int get_graph(int k, bool timed, cudaGraphExec_t* out);
     int dump_files(long itr, double r, double dr);
 };

@@ -1,0 +1,327 @@
+// FP64 per-phase kernel bodies (MA and MAA), shared by the single-simulation
+// kernels (xf_kernels.cu) and the batched kernels (xf_batch.cu).  A body
+// processes beams first, first + stride, ... with one warp per beam and
+// reduces its moments over the RedTarget group.
+#pragma once
+#include "xf_common.cuh"
+
+namespace xf {
+namespace fp64 {
+
+using namespace detail;
+
+constexpr double kSeriesT = 0.25;
+
+// cos(sqrt(t)) and sin(sqrt(t))/sqrt(t) for 0 <= t <= kSeriesT, degree 7 in t.
+// Truncation error below 7.3e-19 (cos) and 4.3e-20 (sinc) at t = 0.25.
+__device__ __forceinline__ void series_cs(double t, double& c, double& s)
+{
+    c = -1.0 / 87178291200.0;
+    c = fma(c, t, 1.0 / 479001600.0);
+    c = fma(c, t, -1.0 / 3628800.0);
+    c = fma(c, t, 1.0 / 40320.0);
+    c = fma(c, t, -1.0 / 720.0);
+    c = fma(c, t, 1.0 / 24.0);
+    c = fma(c, t, -0.5);
+    c = fma(c, t, 1.0);
+    s = -1.0 / 1307674368000.0;
+    s = fma(s, t, 1.0 / 6227020800.0);
+    s = fma(s, t, -1.0 / 39916800.0);
+    s = fma(s, t, 1.0 / 362880.0);
+    s = fma(s, t, -1.0 / 5040.0);
+    s = fma(s, t, 1.0 / 120.0);
+    s = fma(s, t, -1.0 / 6.0);
+    s = fma(s, t, 1.0);
+}
+
+// Coefficients (C, S) of U = C - i S H for H = [[h00, h01],[h01*, -h00]],
+// h01 = h01r + i h01i, over the path length dl: C = cos(lambda dl),
+// S = sin(lambda dl)/lambda, lambda = |H| (src/NBeam.cpp:366-369).
+__device__ __forceinline__ void su2_coeffs(double h00, double h01r, double h01i, double dl, double& C, double& S)
+{
+    const double lam2 = h00 * h00 + (h01r * h01r + h01i * h01i);
+    const double t = lam2 * (dl * dl);
+    if (t <= kSeriesT) {
+        double s;
+        series_cs(t, C, s);
+        S = s * dl;
+    } else {
+        const double lam = sqrt(lam2);
+        double sn, cs;
+        sincos(lam * dl, &sn, &cs);
+        C = cs;
+        S = sn / lam;
+    }
+}
+
+// psi' = U psi with the matrix entries of src/NBeam.cpp:371-392.
+struct Psi {
+    double ar, ai, br, bi;
+};
+
+__device__ __forceinline__ Psi su2_apply(double C, double S, double h00, double h01r, double h01i, const Psi& x)
+{
+    const double m1 = -h00 * S;
+    const double m2 = h01i * S;
+    const double m3 = -h01r * S;
+    Psi y;
+    y.ar = (C * x.ar - m1 * x.ai) + (m2 * x.br - m3 * x.bi);
+    y.ai = (C * x.ai + m1 * x.ar) + (m2 * x.bi + m3 * x.br);
+    y.br = (-m2 * x.ar - m3 * x.ai) + (C * x.br + m1 * x.bi);
+    y.bi = (-m2 * x.ai + m3 * x.ar) + (C * x.bi - m1 * x.br);
+    return y;
+}
+
+// Accumulates fv * rho(psi) (first row of the density matrix, src/NBeam.cpp:314-322);
+// component 0 is accumulated without the factor 1/2, applied once per beam.
+__device__ __forceinline__ void acc_rho(const Psi& x, double fv, double& s0, double& s2, double& s3)
+{
+    const double d0 = (x.ar * x.ar + x.ai * x.ai) - (x.br * x.br + x.bi * x.bi);
+    const double d2 = x.ar * x.br + x.ai * x.bi;
+    const double d3 = x.ai * x.br - x.ar * x.bi;
+    s0 = fma(d0, fv, s0);
+    s2 = fma(d2, fv, s2);
+    s3 = fma(d3, fv, s3);
+}
+
+__device__ __forceinline__ Psi load_psi(const double* __restrict__ base, int epad, int e)
+{
+    Psi x;
+    x.ar = base[e];
+    x.ai = base[epad + e];
+    x.br = base[2 * epad + e];
+    x.bi = base[3 * epad + e];
+    return x;
+}
+
+__device__ __forceinline__ void store_psi(double* __restrict__ base, int epad, int e, const Psi& x)
+{
+    base[e] = x.ar;
+    base[epad + e] = x.ai;
+    base[2 * epad + e] = x.br;
+    base[3 * epad + e] = x.bi;
+}
+
+// ------------------------------------------------------------------ phase A
+
+// S1 (H of psi0 from the cached moments), S2 and S6 (two sweeps sharing H0),
+// and the moments of psi1 at point 2 (S3) and of psi3 at point 1 (S7).
+template <int GEOM>
+__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt)
+{
+    constexpr int K = NK<GEOM>::K;
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    const double* __restrict__ psi0 = ctl->psi0;
+    const double hm = ctl->hm[0];
+    const int lane = threadIdx.x & 31;
+    const int gw = first + (threadIdx.x >> 5), tw = stride;
+    const int epad = d.epad;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    const int myv = lane >> 2;  // value slot owned after an 8-way reduce-scatter
+    for (int b = gw; b < d.nbeams; b += tw) {
+        const BeamIdx bi = decode_beam(d, b);
+        const BeamH h = beam_offsets<GEOM>(d, ctl->J0, 0, hm, bi);
+        const double dl1 = geo(d, 3, 1, bi.ang), dl0 = geo(d, 3, 0, bi.ang);
+        const double* in = psi0 + (size_t)b * 4 * epad;
+        double* o1 = d.psi1 + (size_t)b * 4 * epad;
+        double* o3 = d.psi3 + (size_t)b * 4 * epad;
+        const double* fvp = d.fv + bi.p * epad;
+        double v[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+        for (int e = lane; e < epad; e += 32) {
+            const double h00 = d.hvac[e] + h.h00b;
+            const double h01r = d.hvac[epad + e] + h.h01rb;
+            const Psi x = load_psi(in, epad, e);
+            double C1, S1, C0, S0;
+            if (GEOM == 0) {
+                // MA: dl0 = dl1/2 exactly, so U(dl1) coefficients follow from
+                // the half-length ones by the double-angle identities.
+                su2_coeffs(h00, h01r, h.h01i, dl0, C0, S0);
+                C1 = fma(C0 + C0, C0, -1.0);
+                S1 = (C0 + C0) * S0;
+            } else {
+                su2_coeffs(h00, h01r, h.h01i, dl1, C1, S1);
+                su2_coeffs(h00, h01r, h.h01i, dl0, C0, S0);
+            }
+            const Psi y1 = su2_apply(C1, S1, h00, h01r, h.h01i, x);
+            const Psi y3 = su2_apply(C0, S0, h00, h01r, h.h01i, x);
+            store_psi(o1, epad, e, y1);
+            store_psi(o3, epad, e, y3);
+            const double f = fvp[e];
+            acc_rho(y1, f, v[0], v[1], v[2]);
+            acc_rho(y3, f, v[3], v[4], v[5]);
+        }
+        v[0] *= .5;
+        v[3] *= .5;
+        warp_reduce_scatter<8>(v, lane);
+        if (myv < 3) add_moment<GEOM>(d, v[0], comp_of(myv), 2, bi, acc);
+        else if (myv < 6) add_moment<GEOM>(d, v[0], comp_of(myv - 3), 1, bi, acc);
+    }
+    if (!group_reduce<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
+    if (threadIdx.x < kNJ) {
+        ctl->JA1[threadIdx.x] = 0.;
+        ctl->JA3[threadIdx.x] = 0.;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < 6 * K) {
+        const int v = threadIdx.x / K, k = threadIdx.x % K;
+        double* J = v < 3 ? ctl->JA1 : ctl->JA3;
+        J[k * 4 + comp_of(v % 3)] = s_out[threadIdx.x];
+    }
+}
+
+// ------------------------------------------------------------------ phase B
+
+// S4/S5 (psi4' = U(h1, dl1, hm(r+dr)) psi0 averaged into psi1) and S8
+// (psi4 = U(h3, dl1, hm(r+dr/2)) psi0) with the moments of psi4 at point 2 (S9).
+template <int GEOM>
+__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt)
+{
+    constexpr int K = NK<GEOM>::K;
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    const double* __restrict__ psi0 = ctl->psi0;
+    double* __restrict__ psi4 = ctl->psi4;
+    const double hm_rdr = ctl->hm[2], hm_rdr2 = ctl->hm[1];
+    const int lane = threadIdx.x & 31;
+    const int gw = first + (threadIdx.x >> 5), tw = stride;
+    const int epad = d.epad;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    const int myv = lane >> 3;
+    for (int b = gw; b < d.nbeams; b += tw) {
+        const BeamIdx bi = decode_beam(d, b);
+        const BeamH g1 = beam_offsets<GEOM>(d, ctl->JA1, 2, hm_rdr, bi);
+        const BeamH g3 = beam_offsets<GEOM>(d, ctl->JA3, 1, hm_rdr2, bi);
+        const double dl1 = geo(d, 3, 1, bi.ang);
+        const double* in = psi0 + (size_t)b * 4 * epad;
+        double* io1 = d.psi1 + (size_t)b * 4 * epad;
+        double* o4 = psi4 + (size_t)b * 4 * epad;
+        const double* fvp = d.fv + bi.p * epad;
+        double v[4] = {0., 0., 0., 0.};
+        for (int e = lane; e < epad; e += 32) {
+            const double hv0 = d.hvac[e], hv1 = d.hvac[epad + e];
+            const Psi x = load_psi(in, epad, e);
+            double C, S;
+            const double a00 = hv0 + g1.h00b, a01 = hv1 + g1.h01rb;
+            su2_coeffs(a00, a01, g1.h01i, dl1, C, S);
+            const Psi ya = su2_apply(C, S, a00, a01, g1.h01i, x);
+            const Psi p1 = load_psi(io1, epad, e);
+            Psi avg;
+            avg.ar = (ya.ar + p1.ar) * .5;
+            avg.ai = (ya.ai + p1.ai) * .5;
+            avg.br = (ya.br + p1.br) * .5;
+            avg.bi = (ya.bi + p1.bi) * .5;
+            store_psi(io1, epad, e, avg);
+            const double b00 = hv0 + g3.h00b, b01 = hv1 + g3.h01rb;
+            su2_coeffs(b00, b01, g3.h01i, dl1, C, S);
+            const Psi y4 = su2_apply(C, S, b00, b01, g3.h01i, x);
+            store_psi(o4, epad, e, y4);
+            acc_rho(y4, fvp[e], v[0], v[1], v[2]);
+        }
+        v[0] *= .5;
+        warp_reduce_scatter<4>(v, lane);
+        if (myv < 3) add_moment<GEOM>(d, v[0], comp_of(myv), 2, bi, acc);
+    }
+    if (!group_reduce<K>(rt, 8, 3, acc, 0., false, s_warp, s_out)) return;
+    if (threadIdx.x < kNJ) ctl->JB4[threadIdx.x] = 0.;
+    __syncthreads();
+    if ((int)threadIdx.x < 3 * K) {
+        const int v = threadIdx.x / K, k = threadIdx.x % K;
+        ctl->JB4[k * 4 + comp_of(v)] = s_out[threadIdx.x];
+    }
+}
+
+// ------------------------------------------------------------------ phase C
+
+// S10/S11 (psi3' = U(h4, dl2, hm(r+dr)) psi3; psi4 <- (psi3' + psi4)/2), the
+// error sweep NBeam::calcErrHvv against psi1 (src/NBeam.cpp:903-938) with the
+// max over beams (src/Nmr.cpp:195-206), and the moments of the candidate.
+// Under device control the last block also runs the step controller of
+// src/Nmr.cpp:227-249.
+template <int GEOM>
+__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt)
+{
+    constexpr int K = NK<GEOM>::K;
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    double* __restrict__ psi4 = ctl->psi4;
+    double* __restrict__ S4 = ctl->S4;
+    const double hm_rdr = ctl->hm[2];
+    const int lane = threadIdx.x & 31;
+    const int gw = first + (threadIdx.x >> 5), tw = stride;
+    const int epad = d.epad;
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double mx = -1.0;
+    const int myv = lane >> 3;  // 0: error, 1..3: density components 0, 2, 3
+    for (int b = gw; b < d.nbeams; b += tw) {
+        const BeamIdx bi = decode_beam(d, b);
+        const BeamH g = beam_offsets<GEOM>(d, ctl->JB4, 2, hm_rdr, bi);
+        const double dl2 = geo(d, 3, 2, bi.ang);
+        double* io3 = d.psi3 + (size_t)b * 4 * epad;
+        double* io4 = psi4 + (size_t)b * 4 * epad;
+        const double* p1b = d.psi1 + (size_t)b * 4 * epad;
+        const double* fvp = d.fv + bi.p * epad;
+        double v[4] = {0., 0., 0., 0.};
+        for (int e = lane; e < epad; e += 32) {
+            const double a00 = d.hvac[e] + g.h00b, a01 = d.hvac[epad + e] + g.h01rb;
+            const Psi x3 = load_psi(io3, epad, e);
+            double C, S;
+            su2_coeffs(a00, a01, g.h01i, dl2, C, S);
+            const Psi y3 = su2_apply(C, S, a00, a01, g.h01i, x3);
+            if (d.debug_psi3) store_psi(io3, epad, e, y3);
+            const Psi x4 = load_psi(io4, epad, e);
+            Psi c;
+            c.ar = (y3.ar + x4.ar) * .5;
+            c.ai = (y3.ai + x4.ai) * .5;
+            c.br = (y3.br + x4.br) * .5;
+            c.bi = (y3.bi + x4.bi) * .5;
+            store_psi(io4, epad, e, c);
+            const Psi r1 = load_psi(p1b, epad, e);
+            const double f = fvp[e];
+            const double e0 = c.ar - r1.ar, e1 = c.ai - r1.ai, e2 = c.br - r1.br, e3 = c.bi - r1.bi;
+            v[0] = fma((e0 * e0 + e1 * e1) + (e2 * e2 + e3 * e3), f, v[0]);
+            acc_rho(c, f, v[1], v[2], v[3]);
+        }
+        v[1] *= .5;
+        warp_reduce_scatter<4>(v, lane);
+        if (myv == 0) mx = fmax(mx, v[0]);
+        else add_moment<GEOM>(d, v[0], comp_of(myv - 1), 2, bi, acc);
+        // per-beam moments of the candidate (the reference's hSumMat of psi4)
+        if ((lane & 7) == 0) {
+            if (myv == 0) S4[(size_t)b * 4 + 1] = 0.;
+            else S4[(size_t)b * 4 + comp_of(myv - 1)] = v[0];
+        }
+    }
+    // lanes 8..31 hold moments of slots 1..3; shift them to slots 0..2 for the block reduction
+    double accs[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) accs[k] = __shfl_down_sync(kFull, acc[k], 8);
+    if (!group_reduce<K>(rt, 8, 3, accs, mx, true, s_warp, s_out)) return;
+    if (threadIdx.x < kNJ) ctl->JC[threadIdx.x] = 0.;
+    __syncthreads();
+    if ((int)threadIdx.x < 3 * K) {
+        const int v = threadIdx.x / K, k = threadIdx.x % K;
+        ctl->JC[k * 4 + comp_of(v)] = s_out[threadIdx.x];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double me = sqrt(s_out[31]);
+        ctl->max_err = me;
+        if (d.device_control) step_control(d, ctl, me);
+    }
+}
+
+}  // namespace fp64
+}  // namespace xf

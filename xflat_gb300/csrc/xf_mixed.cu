@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "xf_common.cuh"
+#include "xf_mixed.cuh"
 #include "xf_engine.h"
 #include "xf_kernels.h"
 #include "xf_mixed.h"
@@ -44,470 +45,25 @@ namespace xf {
 namespace {
 
 using namespace detail;
+using mixed::KSum;
+// ------------------------------------------------------------------ phases
 
-constexpr float kSeriesTF = 1.0f;
-
-// Taylor coefficients of cos(x) - 1 = sum_{k>=1} c_k t^k and
-// sin(x)/x = sum_{k>=0} s_k t^k, t = x^2; degree 5 keeps the truncation below
-// 4e-9 relative for t <= 1.
-__constant__ float kC[6] = {0.f, -0.5f, 1.f / 24.f, -1.f / 720.f, 1.f / 40320.f, -1.f / 3628800.f};
-__constant__ float kS[6] = {1.f, -1.f / 6.f, 1.f / 120.f, -1.f / 5040.f, 1.f / 362880.f, -1.f / 39916800.f};
-__device__ __forceinline__ float horner(const float* c, float t)
-{
-    float p = c[5];
-    p = fmaf(p, t, c[4]);
-    p = fmaf(p, t, c[3]);
-    p = fmaf(p, t, c[2]);
-    p = fmaf(p, t, c[1]);
-    return fmaf(p, t, c[0]);
-}
-
-// p(tB) and the divided difference p[tA, tB] = (p(tA) - p(tB)) / (tA - tB).
-__device__ __forceinline__ void divdiff(const float* c, float tA, float tB, float& pB, float& dd)
-{
-    float P = c[5], D = 0.f;
-#pragma unroll
-    for (int k = 4; k >= 0; --k) {
-        D = fmaf(D, tA, P);
-        P = fmaf(P, tB, c[k]);
-    }
-    pB = P;
-    dd = D;
-}
-
-struct H3f {
-    float h00, h01r, h01i;
-};
-
-struct F4 {
-    float ar, ai, br, bi;
-};
-
-__device__ __forceinline__ float norm2(const H3f& h) { return h.h00 * h.h00 + (h.h01r * h.h01r + h.h01i * h.h01i); }
-
-// u = sigma(h) psi for sigma(h) = [[h00, h01r + i h01i], [h01r - i h01i, -h00]]
-// (the Hamiltonian matrix of src/NBeam.cpp:371-392).
-__device__ __forceinline__ F4 sig_apply(const H3f& h, const F4& x)
-{
-    F4 u;
-    u.ar = h.h00 * x.ar + h.h01r * x.br - h.h01i * x.bi;
-    u.ai = h.h00 * x.ai + h.h01r * x.bi + h.h01i * x.br;
-    u.br = h.h01r * x.ar + h.h01i * x.ai - h.h00 * x.br;
-    u.bi = h.h01r * x.ai - h.h01i * x.ar - h.h00 * x.bi;
-    return u;
-}
-
-// c psi - i v  with v given as the complex vector (v.ar + i v.ai, v.br + i v.bi)
-__device__ __forceinline__ F4 combine(float c, const F4& x, const F4& v)
-{
-    F4 y;
-    y.ar = c * x.ar + v.ai;
-    y.ai = c * x.ai - v.ar;
-    y.br = c * x.br + v.bi;
-    y.bi = c * x.bi - v.br;
-    return y;
-}
-
-__device__ __forceinline__ F4 scale(float s, const F4& u)
-{
-    F4 v;
-    v.ar = s * u.ar;
-    v.ai = s * u.ai;
-    v.br = s * u.br;
-    v.bi = s * u.bi;
-    return v;
-}
-
-__device__ __forceinline__ F4 add(const F4& a, const F4& b)
-{
-    F4 c;
-    c.ar = a.ar + b.ar;
-    c.ai = a.ai + b.ai;
-    c.br = a.br + b.br;
-    c.bi = a.bi + b.bi;
-    return c;
-}
-
-// K = (C - 1) - i S sigma(h) over the path length l.
-struct KC {
-    float cm1, S;
-};
-
-__device__ __forceinline__ KC kcoef(const H3f& h, float l)
-{
-    const float t = norm2(h) * (l * l);
-    KC k;
-    if (t <= kSeriesTF) {
-        k.cm1 = horner(kC, t);
-        k.S = l * horner(kS, t);
-    } else {
-        const float x = sqrtf(t);
-        float s, c;
-        sincosf(x, &s, &c);
-        k.cm1 = c - 1.f;
-        k.S = l * (s / x);
-    }
-    return k;
-}
-
-__device__ __forceinline__ F4 k_apply(const KC& k, const H3f& h, const F4& x)
-{
-    return combine(k.cm1, x, scale(k.S, sig_apply(h, x)));
-}
-
-// [K(hA, l) - K(hB, l)] x given the accurate difference dh = hA - hB.
-__device__ __forceinline__ F4 diff_h(const H3f& hA, const H3f& hB, const H3f& dh, float l, const F4& x)
-{
-    const float l2 = l * l;
-    const float tA = norm2(hA) * l2, tB = norm2(hB) * l2;
-    if (tA > kSeriesTF || tB > kSeriesTF) {
-        const F4 a = k_apply(kcoef(hA, l), hA, x), b = k_apply(kcoef(hB, l), hB, x);
-        F4 r;
-        r.ar = a.ar - b.ar;
-        r.ai = a.ai - b.ai;
-        r.br = a.br - b.br;
-        r.bi = a.bi - b.bi;
-        return r;
-    }
-    const float dt = l2 * (dh.h00 * (hA.h00 + hB.h00) + dh.h01r * (hA.h01r + hB.h01r) + dh.h01i * (hA.h01i + hB.h01i));
-    float cB, dc, sB, ds;
-    divdiff(kC, tA, tB, cB, dc);
-    divdiff(kS, tA, tB, sB, ds);
-    const float SA = l * fmaf(dt, ds, sB);
-    const float dS = l * (dt * ds);
-    const F4 v = add(scale(SA, sig_apply(dh, x)), scale(dS, sig_apply(hB, x)));
-    return combine(dt * dc, x, v);
-}
-
-// [K(h, lA) - K(h, lB)] x given the accurate difference dl = lA - lB.
-__device__ __forceinline__ F4 diff_l(const H3f& h, float lA, float lB, float dl, const F4& x)
-{
-    const float n2 = norm2(h);
-    const float tA = n2 * lA * lA, tB = n2 * lB * lB;
-    if (tA > kSeriesTF || tB > kSeriesTF) {
-        const F4 a = k_apply(kcoef(h, lA), h, x), b = k_apply(kcoef(h, lB), h, x);
-        F4 r;
-        r.ar = a.ar - b.ar;
-        r.ai = a.ai - b.ai;
-        r.br = a.br - b.br;
-        r.bi = a.bi - b.bi;
-        return r;
-    }
-    const float dt = n2 * dl * (lA + lB);
-    float cB, dc, sB, ds;
-    divdiff(kC, tA, tB, cB, dc);
-    divdiff(kS, tA, tB, sB, ds);
-    const float sA = fmaf(dt, ds, sB);
-    const float dS = fmaf(dl, sA, lB * (dt * ds));
-    return combine(dt * dc, x, scale(dS, sig_apply(h, x)));
-}
-
-// Kahan-compensated FP32 accumulation (per thread, over its energies).
-struct KSum {
-    float s, c;
-    __device__ __forceinline__ void add(float v)
-    {
-        const float y = v - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
-// fv * [rho(x + d) - rho(x)] (first row of the density matrix, src/NBeam.cpp:314-322;
-// component 0 without the factor 1/2): only the cross and quadratic terms in
-// the increment d, so the FP32 result is precise relative to the increment.
-__device__ __forceinline__ void acc_drho(const F4& x, const F4& dd, float fv, KSum& s0, KSum& s2, KSum& s3)
-{
-    const F4 y = add(x, dd);
-    const float r0 = (dd.ar * (x.ar + y.ar) + dd.ai * (x.ai + y.ai)) - (dd.br * (x.br + y.br) + dd.bi * (x.bi + y.bi));
-    const float r2 = (dd.ar * y.br + dd.ai * y.bi) + (x.ar * dd.br + x.ai * dd.bi);
-    const float r3 = (dd.ai * y.br - dd.ar * y.bi) + (x.ai * dd.br - x.ar * dd.bi);
-    s0.add(r0 * fv);
-    s2.add(r2 * fv);
-    s3.add(r3 * fv);
-}
-
-__device__ __forceinline__ F4 load_f(const float* __restrict__ b, int epad, int e)
-{
-    F4 x;
-    x.ar = b[e];
-    x.ai = b[epad + e];
-    x.br = b[2 * epad + e];
-    x.bi = b[3 * epad + e];
-    return x;
-}
-
-__device__ __forceinline__ void store_f(float* __restrict__ b, int epad, int e, const F4& x)
-{
-    b[e] = x.ar;
-    b[epad + e] = x.ai;
-    b[2 * epad + e] = x.br;
-    b[3 * epad + e] = x.bi;
-}
-
-// (hi, lo) + d as an FP32 pair: TwoSum of hi and d, then a renormalising
-// Fast2Sum of the result with the accumulated low parts.
-__device__ __forceinline__ void ff_add(float hi, float lo, float d, float& nhi, float& nlo)
-{
-    const float s = hi + d;
-    const float bp = s - hi;
-    const float e = ((hi - (s - bp)) + (d - bp)) + lo;
-    nhi = s + e;
-    nlo = e - (nhi - s);
-}
-
-__device__ __forceinline__ H3f bin_h(const BeamH& b, float hv0, float hv1)
-{
-    H3f h;
-    h.h00 = hv0 + (float)b.h00b;
-    h.h01r = hv1 + (float)b.h01rb;
-    h.h01i = (float)b.h01i;
-    return h;
-}
-
-__device__ __forceinline__ H3f diff_beam(const BeamH& a, const BeamH& b)
-{
-    H3f d;
-    d.h00 = (float)(a.h00b - b.h00b);
-    d.h01r = (float)(a.h01rb - b.h01rb);
-    d.h01i = (float)(a.h01i - b.h01i);
-    return d;
-}
-
-// Per-beam energy sum of a stage state = the exact FP64 sum of psi0 (S0) plus
-// the reduced increment sum; lanes own value slots after the reduce-scatter.
-__device__ __forceinline__ double stage_sum(const double* S0, int b, int comp, double inc)
-{
-    return S0[(size_t)b * 4 + comp] + inc;
-}
-
-// ------------------------------------------------------------------ phase A
-
-// Moments of psi1 = U(h0, dl1) psi0 at point 2 and of psi3 = U(h0, dl0) psi0 at point 1.
 template <int GEOM>
 __global__ void __launch_bounds__(256) k_mixA(Dev d)
 {
-    constexpr int K = NK<GEOM>::K;
-    Ctl* ctl = d.ctl;
-    if (ctl->done) return;
-    __shared__ double s_warp[8 * 32];
-    __shared__ double s_out[32];
-    const float* __restrict__ p0 = ctl->m0hi;
-    const double* __restrict__ S0 = ctl->S0;
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int gw = blockIdx.x * nw + (threadIdx.x >> 5), tw = gridDim.x * nw;
-    const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
-    const int myv = lane >> 2;
-    for (int b = gw; b < d.nbeams; b += tw) {
-        const BeamIdx bi = decode_beam(d, b);
-        const BeamH g0 = beam_offsets<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi);
-        const float l1 = (float)geo(d, 3, 1, bi.ang), l0 = (float)geo(d, 3, 0, bi.ang);
-        const float* in = p0 + (size_t)b * 4 * epad;
-        const float* fvp = d.fvf + bi.p * epad;
-        KSum s[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) s[i] = KSum{0.f, 0.f};
-        for (int e = lane; e < epad; e += 32) {
-            const H3f h = bin_h(g0, d.hvf[e], d.hvf[epad + e]);
-            const F4 x = load_f(in, epad, e);
-            const KC k0 = kcoef(h, l0);
-            KC k1;
-            if (GEOM == 0) {
-                // MA: dl1 = 2 dl0, so C1 - 1 = 2 (C0 - 1)(C0 + 1) and S1 = 2 C0 S0
-                k1.cm1 = 2.f * k0.cm1 * (k0.cm1 + 2.f);
-                k1.S = 2.f * (1.f + k0.cm1) * k0.S;
-            } else {
-                k1 = kcoef(h, l1);
-            }
-            const F4 u = sig_apply(h, x);
-            const F4 d1 = combine(k1.cm1, x, scale(k1.S, u));
-            const F4 d3 = combine(k0.cm1, x, scale(k0.S, u));
-            const float f = fvp[e];
-            acc_drho(x, d1, f, s[0], s[1], s[2]);
-            acc_drho(x, d3, f, s[3], s[4], s[5]);
-        }
-        double v[8];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) v[i] = s[i].value();
-        v[6] = v[7] = 0.;
-        v[0] *= .5;
-        v[3] *= .5;
-        warp_reduce_scatter<8>(v, lane);
-        if (myv < 3) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv), v[0]), comp_of(myv), 2, bi, acc);
-        else if (myv < 6) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv - 3), v[0]), comp_of(myv - 3), 1, bi, acc);
-    }
-    if (!block_and_grid_reduce<K>(d, PH_A, 4, 6, acc, 0., false, s_warp, s_out)) return;
-    if (threadIdx.x < kNJ) {
-        ctl->JA1[threadIdx.x] = 0.;
-        ctl->JA3[threadIdx.x] = 0.;
-    }
-    __syncthreads();
-    if ((int)threadIdx.x < 6 * K) {
-        const int v = threadIdx.x / K, k = threadIdx.x % K;
-        double* J = v < 3 ? ctl->JA1 : ctl->JA3;
-        J[k * 4 + comp_of(v % 3)] = s_out[threadIdx.x];
-    }
+    mixed::phaseA_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_A));
 }
 
-// ------------------------------------------------------------------ phase B
-
-// Moments of psi4 = U(h3, dl1) psi0 at point 2.
 template <int GEOM>
 __global__ void __launch_bounds__(256) k_mixB(Dev d)
 {
-    constexpr int K = NK<GEOM>::K;
-    Ctl* ctl = d.ctl;
-    if (ctl->done) return;
-    __shared__ double s_warp[8 * 32];
-    __shared__ double s_out[32];
-    const float* __restrict__ p0 = ctl->m0hi;
-    const double* __restrict__ S0 = ctl->S0;
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int gw = blockIdx.x * nw + (threadIdx.x >> 5), tw = gridDim.x * nw;
-    const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
-    const int myv = lane >> 3;
-    for (int b = gw; b < d.nbeams; b += tw) {
-        const BeamIdx bi = decode_beam(d, b);
-        const BeamH g3 = beam_offsets<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi);
-        const float l1 = (float)geo(d, 3, 1, bi.ang);
-        const float* in = p0 + (size_t)b * 4 * epad;
-        const float* fvp = d.fvf + bi.p * epad;
-        KSum s0{0.f, 0.f}, s2{0.f, 0.f}, s3{0.f, 0.f};
-        for (int e = lane; e < epad; e += 32) {
-            const H3f h = bin_h(g3, d.hvf[e], d.hvf[epad + e]);
-            const F4 x = load_f(in, epad, e);
-            acc_drho(x, k_apply(kcoef(h, l1), h, x), fvp[e], s0, s2, s3);
-        }
-        double v[4] = {.5 * s0.value(), s2.value(), s3.value(), 0.};
-        warp_reduce_scatter<4>(v, lane);
-        if (myv < 3) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv), v[0]), comp_of(myv), 2, bi, acc);
-    }
-    if (!block_and_grid_reduce<K>(d, PH_B, 8, 3, acc, 0., false, s_warp, s_out)) return;
-    if (threadIdx.x < kNJ) ctl->JB4[threadIdx.x] = 0.;
-    __syncthreads();
-    if ((int)threadIdx.x < 3 * K) {
-        const int v = threadIdx.x / K, k = threadIdx.x % K;
-        ctl->JB4[k * 4 + comp_of(v)] = s_out[threadIdx.x];
-    }
+    mixed::phaseB_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_B));
 }
 
-// ------------------------------------------------------------------ phase C
-
-// Candidate psi4 = psi0 + (d3' + d4m)/2 with d3 = K(h0,l0) psi0,
-// d3' = d3 + K(h4,l2)(psi0 + d3), d4m = K(h3,l1) psi0; the error estimate in
-// difference form; moments of the candidate; the step controller.
 template <int GEOM>
 __global__ void __launch_bounds__(256) k_mixC(Dev d)
 {
-    constexpr int K = NK<GEOM>::K;
-    Ctl* ctl = d.ctl;
-    if (ctl->done) return;
-    __shared__ double s_warp[8 * 32];
-    __shared__ double s_out[32];
-    const float* __restrict__ hi0 = ctl->m0hi;
-    const float* __restrict__ lo0 = ctl->m0lo;
-    float* __restrict__ hi4 = ctl->m4hi;
-    float* __restrict__ lo4 = ctl->m4lo;
-    const double* __restrict__ S0 = ctl->S0;
-    double* __restrict__ S4 = ctl->S4;
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int gw = blockIdx.x * nw + (threadIdx.x >> 5), tw = gridDim.x * nw;
-    const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
-    double mx = -1.0;
-    const int myv = lane >> 3;
-    for (int b = gw; b < d.nbeams; b += tw) {
-        const BeamIdx bi = decode_beam(d, b);
-        const BeamH g0 = beam_offsets<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi);
-        const BeamH g1 = beam_offsets<GEOM>(d, ctl->JA1, 2, ctl->hm[2], bi);
-        const BeamH g3 = beam_offsets<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi);
-        const BeamH g4 = beam_offsets<GEOM>(d, ctl->JB4, 2, ctl->hm[2], bi);
-        const H3f d31 = diff_beam(g3, g1), d40 = diff_beam(g4, g0);
-        const double L0 = geo(d, 3, 0, bi.ang), L1 = geo(d, 3, 1, bi.ang), L2 = geo(d, 3, 2, bi.ang);
-        const float l0 = (float)L0, l1 = (float)L1, l2 = (float)L2;
-        const float dl20 = (float)(L2 - L0);
-        const float dl01 = (float)(2.0 * L0 - L1);  // zero in MA
-        const size_t base = (size_t)b * 4 * epad;
-        const float* fvp = d.fvf + bi.p * epad;
-        KSum s0{0.f, 0.f}, s2{0.f, 0.f}, s3{0.f, 0.f};
-        float err = 0.f;
-        for (int e = lane; e < epad; e += 32) {
-            const float hv0 = d.hvf[e], hv1 = d.hvf[epad + e];
-            const H3f h0 = bin_h(g0, hv0, hv1), h1 = bin_h(g1, hv0, hv1);
-            const H3f h3 = bin_h(g3, hv0, hv1), h4 = bin_h(g4, hv0, hv1);
-            const F4 x = load_f(hi0 + base, epad, e);
-            const KC k0 = kcoef(h0, l0), k4 = kcoef(h4, l2), k3 = kcoef(h3, l1);
-            const F4 d3 = k_apply(k0, h0, x);
-            const F4 x3 = add(x, d3);
-            const F4 d3p = add(d3, k_apply(k4, h4, x3));
-            const F4 d4m = k_apply(k3, h3, x);
-            F4 inc;
-            inc.ar = .5f * (d3p.ar + d4m.ar);
-            inc.ai = .5f * (d3p.ai + d4m.ai);
-            inc.br = .5f * (d3p.br + d4m.br);
-            inc.bi = .5f * (d3p.bi + d4m.bi);
-            // candidate as a compensated pair
-            const F4 xl = load_f(lo0 + base, epad, e);
-            F4 ch, cl;
-            ff_add(x.ar, xl.ar, inc.ar, ch.ar, cl.ar);
-            ff_add(x.ai, xl.ai, inc.ai, ch.ai, cl.ai);
-            ff_add(x.br, xl.br, inc.br, ch.br, cl.br);
-            ff_add(x.bi, xl.bi, inc.bi, ch.bi, cl.bi);
-            store_f(hi4 + base, epad, e, ch);
-            store_f(lo4 + base, epad, e, cl);
-            // 2 delta = psi4 - psi1 in difference form (see the file header)
-            F4 t2 = diff_h(h3, h1, d31, l1, x);
-            t2 = add(t2, diff_h(h4, h0, d40, l2, x3));
-            t2 = add(t2, diff_l(h0, l2, l0, dl20, x3));
-            if (GEOM == 1) t2 = add(t2, diff_l(h0, 2.f * l0, l1, dl01, x));
-            const float f = fvp[e];
-            err = fmaf(.25f * ((t2.ar * t2.ar + t2.ai * t2.ai) + (t2.br * t2.br + t2.bi * t2.bi)), f, err);
-            acc_drho(x, inc, f, s0, s2, s3);
-        }
-        double v[4] = {(double)err, .5 * s0.value(), s2.value(), s3.value()};
-        warp_reduce_scatter<4>(v, lane);
-        double sv = v[0];
-        if (myv > 0) sv = stage_sum(S0, b, comp_of(myv - 1), v[0]);
-        if (myv == 0) mx = fmax(mx, v[0]);
-        else add_moment<GEOM>(d, sv, comp_of(myv - 1), 2, bi, acc);
-        if ((lane & 7) == 0) {
-            if (myv == 0) S4[(size_t)b * 4 + 1] = 0.;
-            else S4[(size_t)b * 4 + comp_of(myv - 1)] = sv;
-        }
-    }
-    double accs[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) accs[k] = __shfl_down_sync(kFull, acc[k], 8);
-    if (!block_and_grid_reduce<K>(d, PH_C, 8, 3, accs, mx, true, s_warp, s_out)) return;
-    if (threadIdx.x < kNJ) ctl->JC[threadIdx.x] = 0.;
-    __syncthreads();
-    if ((int)threadIdx.x < 3 * K) {
-        const int v = threadIdx.x / K, k = threadIdx.x % K;
-        ctl->JC[k * 4 + comp_of(v)] = s_out[threadIdx.x];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const double me = sqrt(s_out[31]);
-        ctl->max_err = me;
-        if (d.device_control && step_control(d, ctl, me)) {
-            float* t = ctl->m0hi;
-            ctl->m0hi = ctl->m4hi;
-            ctl->m4hi = t;
-            t = ctl->m0lo;
-            ctl->m0lo = ctl->m4lo;
-            ctl->m4lo = t;
-        }
-    }
+    mixed::phaseC_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_C));
 }
 
 // ------------------------------------------------------------------ helpers
@@ -519,47 +75,7 @@ __global__ void __launch_bounds__(256) k_mixC(Dev d)
 // renormalisation (every renorm_every accepted steps under device control).
 __global__ void __launch_bounds__(256) k_mix_esum(Dev d, int renorm, int conditional)
 {
-    Ctl* ctl = d.ctl;
-    if (conditional && !ctl->renorm_due) return;
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int gw = blockIdx.x * nw + (threadIdx.x >> 5), tw = gridDim.x * nw;
-    const int epad = d.epad;
-    float* hi = ctl->m0hi;
-    float* lo = ctl->m0lo;
-    double* S = ctl->S0;
-    for (int b = gw; b < d.nbeams; b += tw) {
-        float* ph = hi + (size_t)b * 4 * epad;
-        float* pl = lo + (size_t)b * 4 * epad;
-        const double* fvp = d.fv + (b & 3) * epad;
-        double v[4] = {0., 0., 0., 0.};
-        for (int e = lane; e < epad; e += 32) {
-            double a[4];
-            double n = 0.;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                a[k] = (double)ph[k * epad + e] + (double)pl[k * epad + e];
-                n = fma(a[k], a[k], n);
-            }
-            if (renorm && n > 0.) {
-                const double f = 1. / sqrt(n);
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    a[k] *= f;
-                    const float ah = (float)a[k];
-                    ph[k * epad + e] = ah;
-                    pl[k * epad + e] = (float)(a[k] - (double)ah);
-                }
-            }
-            const double fe = fvp[e];
-            v[1] = fma((a[0] * a[0] + a[1] * a[1]) - (a[2] * a[2] + a[3] * a[3]), fe, v[1]);
-            v[2] = fma(a[0] * a[2] + a[1] * a[3], fe, v[2]);
-            v[3] = fma(a[1] * a[2] - a[0] * a[3], fe, v[3]);
-        }
-        v[1] *= .5;
-        warp_reduce_scatter<4>(v, lane);
-        const int myv = lane >> 3;
-        if ((lane & 7) == 0) S[(size_t)b * 4 + (myv == 0 ? 1 : comp_of(myv - 1))] = (myv == 0) ? 0. : v[0];
-    }
+    mixed::esum_body(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), renorm, conditional);
 }
 
 // Accept under host control: swap the state, sum and moment roles.
