@@ -254,6 +254,7 @@ def ours(args, rank, world, dist):
     # --- mixed precision on the same workload (FP32 rotations and compensated
     # FP32 state, FP64 reductions/control): same start state, same K steps
     mixed = mixed_leg(xg, text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
+    batched = batched_leg(xg, args.batch_steps) if args.batch_steps > 0 else None
 
     # --- end to end through the C ABI with host buffers: state H2D from pinned
     # memory, the host-driven reference loop (per step: r, dr and the three
@@ -316,7 +317,7 @@ def ours(args, rank, world, dist):
                                   "frac": hbm_achieved / hbm_peak if hbm_peak else None,
                                   "algorithmic_bytes_per_bin": PHASE_BYTES[dom]}},
         "phases_ms": {p: phase_ms[i] for i, p in enumerate("ABC")},
-        "variants": {"fp64": {"value": value, "unit": UNIT}, "mixed": mixed},
+        "variants": {"fp64": {"value": value, "unit": UNIT}, "mixed": mixed, "batched": batched},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": (state_bytes + 40 * e["iterations"]) /
                 max(1, e["iterations"]), "d2h_bytes_per_step": (state_bytes + 8 * e["iterations"]) /
@@ -354,6 +355,43 @@ def mixed_leg(xg, text, psi_start, r0, dr0, steps, bins, psi_fp64_end, surv_fp64
     return res
 
 
+def batched_leg(xg, steps):
+    """The batched parameter sweep (64 independent MA instances from a seed,
+    xflat_gb300.sweep): mixed precision and FP64 in one batch each, and the same
+    64 instances run back to back through the single-simulation FP64 path."""
+    import numpy as np
+    from xflat_gb300.sweep import sweep_configs
+    out = {"workload": "64 MA instances (seed 4): angle bins U{128..2048}, energy bins U{32..512} (1-60 MeV), "
+                       "L log-U[1e50,1e52] erg/s, NH/IH p=1/2, lambda0 log-U[1e2,1e4] /km, from r=10 km",
+           "steps_per_instance": steps}
+    states = {}
+    for prec in ("mixed", "fp64"):
+        b = xg.Batch([xg.Config.from_text(t) for t in sweep_configs(seed=4, n=64, precision=prec)])
+        r = b.run(max_iters=steps)
+        units = sum(nb * ne * i for (nb, ne), i in zip(b.dims, r["iterations"]))
+        out["bins"] = sum(nb * ne for nb, ne in b.dims)
+        out["batched_" + prec] = {"value": units / r["seconds"], "unit": UNIT, "tile_warps": b.tile_shape()[0],
+                                  "seconds": r["seconds"]}
+        states[prec] = ([b.get_state(i)[0::4, :2] for i in range(len(b.dims))], list(r["accepted"]))
+        b.close()
+    units, ms = 0, 0.0
+    for t in sweep_configs(seed=4, n=64, precision="fp64"):
+        s = xg.Simulation(xg.Config.from_text(t))
+        o = s.evolutionLoop(max_iters=steps, device_control=True)
+        units += s.nbeams * s.ebins * o["iterations"]
+        ms += o["device_ms"]
+        s.close()
+    out["fp64_back_to_back"] = {"value": units / (ms * 1e-3), "unit": UNIT}
+    out["speedup_batched_mixed_vs_fp64_back_to_back"] = out["batched_mixed"]["value"] / out["fp64_back_to_back"]["value"]
+    d = []
+    for a, c, na, nc in zip(states["fp64"][0], states["mixed"][0], states["fp64"][1], states["mixed"][1]):
+        if na == nc:
+            d.append(np.max(np.abs((a[:, 0] ** 2 + a[:, 1] ** 2) - (c[:, 0] ** 2 + c[:, 1] ** 2))))
+    out["max_dPee_batched_mixed_vs_fp64"] = float(max(d)) if d else None
+    out["instances_compared"] = len(d)
+    return out
+
+
 def lib_peak(lib):
     import ctypes
     v = ctypes.c_double()
@@ -368,6 +406,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
+    ap.add_argument("--batch-steps", type=int, default=24, help="iterations per instance of the batched legs (0 = skip)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

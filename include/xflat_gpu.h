@@ -211,6 +211,31 @@ int xf_calc_hvv_static(int geometry, int abins, int pbins, int ebins, int epad, 
  * blocks per SM) for about `ms` milliseconds: *tflops = 2 flops per FMA. */
 int xf_probe_fp64_peak(double ms, double* tflops);
 
+/* ---------------------------------------------------------------- files */
+/* The reference's NetCDF IO module (src/IO_f.cpp), written without libnetcdf
+ * in the classic format (64-bit offsets): file names <prefix>Snapshot<n>_0_.nc
+ * (dims r[unlimited], theta, [phi], prtcl, comp, ebin; variables r, dr, psi)
+ * and <prefix>Probability<n>_0_.nc (dims r, theta, phi; variables r,
+ * prtcl0..prtcl3).
+ * xf_dump: fio::dumpToFile (src/IO_f.cpp:387-424) with the same radius, time
+ *   and iteration triggers, file rotation every new_file_step records and
+ *   sync every sync_step; files are created on the first call.
+ * xf_resume: fio::fillInitData (src/IO_f.cpp:197-250): psi0 and the last r
+ *   and dr from the last record of a Snapshot file.
+ * xf_io_close: fio::freemem (src/IO_f.cpp:252-263).
+ * xf_io_verbose: print the radius on dumps, as the reference does (default off). */
+int xf_dump(xf_handle* h, long itr, double r, double dr);
+int xf_resume(xf_handle* h, const char* path, double* r, double* dr);
+int xf_io_close(xf_handle* h);
+int xf_io_verbose(xf_handle* h, int on);
+/* Host-only (no GPU): write a Snapshot file with nrec records from host arrays
+ * (psi: nrec x [beam][comp][ebin]) for configuration cfg, and read record rec
+ * (< 0: the last) of one; *nrec receives the record count.  Any output may be
+ * NULL. */
+int xf_snapshot_write(const char* path, const xf_config* cfg, long nrec, const double* r, const double* dr,
+                      const double* psi);
+int xf_snapshot_read(const char* path, long rec, double* r, double* dr, double* psi, long* nrec);
+
 /* ---------------------------------------------------------------- batch */
 /* Many independent simulations with per-instance adaptive steps, advanced
  * together by the same phase kernels (one launch per phase covers every

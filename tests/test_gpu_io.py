@@ -1,0 +1,91 @@
+"""Snapshot/Probability output during a run, resume from a snapshot, and the
+xflat_gpu command-line driver (src/main.cpp argv contract)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import xflat_gb300 as xg
+from helpers import ROOT, derive, pol_rel_err
+
+pytestmark = pytest.mark.gpu
+scipy_io = pytest.importorskip("scipy.io")
+
+
+def _cfg(tmp_path, dump_mode=3, **over):
+    kv = dict(Abins=8, Ebins=16, R0=20, dr="1e-5", dumpMode=dump_mode, r_step1="0.00005", r_step2="0.00005",
+              filePrefix=str(tmp_path) + "/run")
+    kv.update(over)
+    return derive("config0_ma.txt", **kv)
+
+
+def test_dumps_during_run(tmp_path):
+    text = _cfg(tmp_path)
+    sim = xg.Simulation(xg.Config.from_text(text))
+    o = xg._abi.XfRunOpts()
+    lib = sim.lib
+    lib.xf_run_opts_default(o)
+    o.max_iters = 60
+    o.write_files = 1
+    st = xg._abi.XfRunStats()
+    assert lib.xf_run(sim.h, o, xg._abi.XF_STEP_CB(0), None, st) == 0
+    assert lib.xf_io_close(sim.h) == 0
+    snap = str(tmp_path / "runSnapshot0_0_.nc")
+    prob = str(tmp_path / "runProbability0_0_.nc")
+    with scipy_io.netcdf_file(snap, "r", mmap=False) as f:
+        n = f.variables["r"].shape[0]
+        assert n >= 2
+        last = f.variables["psi"][n - 1].reshape(sim.nbeams, 4, sim.ebins)
+        assert np.array_equal(last, sim.get_state(0))
+        assert f.variables["r"][n - 1] == st.r_end
+    with scipy_io.netcdf_file(prob, "r", mmap=False) as f:
+        m = f.variables["r"].shape[0]
+        sv = sim.survival()
+        for p in range(4):
+            np.testing.assert_allclose(f.variables["prtcl%d" % p][m - 1].reshape(-1), sv[:, p], rtol=1e-15)
+
+
+def test_resume_continues_the_run(tmp_path):
+    text = _cfg(tmp_path, dump_mode=1)
+    a = xg.Simulation(xg.Config.from_text(text))
+    o = xg._abi.XfRunOpts()
+    a.lib.xf_run_opts_default(o)
+    o.max_iters = 40
+    o.write_files = 1
+    st = xg._abi.XfRunStats()
+    assert a.lib.xf_run(a.h, o, xg._abi.XF_STEP_CB(0), None, st) == 0
+    a.lib.xf_io_close(a.h)
+    snap = str(tmp_path / "runSnapshot0_0_.nc")
+    with scipy_io.netcdf_file(snap, "r", mmap=False) as f:
+        r_last = float(f.variables["r"][-1])
+        dr_last = float(f.variables["dr"][-1])
+        psi_last = f.variables["psi"][-1].reshape(a.nbeams, 4, a.ebins).copy()
+    b = xg.Simulation(xg.Config.from_text(text.replace("dumpMode= 1", "dumpMode= 0")))
+    r, dr = xg._abi.ctypes.c_double(), xg._abi.ctypes.c_double()
+    assert b.lib.xf_resume(b.h, snap.encode(), r, dr) == 0
+    assert r.value == r_last and dr.value == dr_last
+    assert np.array_equal(b.get_state(0), psi_last)
+    # the reference resumes with dr as stored (src/IO_f.cpp:214-217)
+    c = xg.Simulation(xg.Config.from_text(text.replace("dumpMode= 1", "dumpMode= 0")))
+    c.set_state(psi_last)
+    ob = b.evolutionLoop(max_iters=20, r0=r.value, dr0=dr.value)
+    oc = c.evolutionLoop(max_iters=20, r0=r_last, dr0=dr_last)
+    assert ob["accepted"] == oc["accepted"]
+    assert pol_rel_err(b.get_state(0), c.get_state(0)) <= 1e-14
+    bad = xg.Simulation(xg.Config.from_text(derive("config0_ma.txt", Abins=9, Ebins=16)))
+    assert bad.lib.xf_resume(bad.h, snap.encode(), r, dr) == xg._abi.XF_EINVAL
+
+
+def test_command_line_driver(tmp_path):
+    text = _cfg(tmp_path, dump_mode=1, Ts=30)
+    cfg = tmp_path / "c.txt"
+    cfg.write_text(text)
+    exe = os.path.join(ROOT, "xflat_gb300", "_lib", "xflat_gpu")
+    out = subprocess.run([exe, str(cfg)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert "Total iterations: 30" in out.stdout
+    snap = tmp_path / "runSnapshot0_0_.nc"
+    assert snap.exists()
+    out2 = subprocess.run([exe, str(cfg), str(snap)], capture_output=True, text=True, timeout=120)
+    assert out2.returncode == 0 and "Provided data file" in out2.stdout

@@ -94,6 +94,14 @@ PROTOTYPES = {
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double_p,
                                           ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]),
+    "xf_dump": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_long, ctypes.c_double, ctypes.c_double]),
+    "xf_resume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, c_double_p, c_double_p]),
+    "xf_io_close": (ctypes.c_int, [ctypes.c_void_p]),
+    "xf_io_verbose": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "xf_snapshot_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(XfConfig), ctypes.c_long, c_double_p,
+                                         c_double_p, c_double_p]),
+    "xf_snapshot_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_long, c_double_p, c_double_p, c_double_p,
+                                        c_long_p]),
     "xf_batch_create": (ctypes.c_int, [ctypes.POINTER(XfConfig), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "xf_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "xf_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),

@@ -179,6 +179,7 @@ int xf_handle::init(const xf_config& c)
 
 void xf_handle::release()
 {
+    xf_io_close(this);
     if (mixed) xf::mixed_destroy(mixed);
     mixed = nullptr;
     for (auto& g : graphs)
@@ -546,13 +547,6 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     return XF_OK;
 }
 
-int xf_handle::dump_files(long itr, double r, double dr)
-{
-    (void)itr;
-    (void)r;
-    (void)dr;
-    return XF_OK;
-}
 
 // ------------------------------------------------------------------ C ABI
 

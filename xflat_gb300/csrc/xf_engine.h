@@ -13,6 +13,7 @@
 namespace xf {
 struct Mixed;  // mixed-precision state (xf_mixed.cu)
 }
+struct xf_io;  // Snapshot / Probability files (xf_io.cpp)
 
 struct xf_handle {
     xf_config cfg{};
@@ -46,6 +47,7 @@ struct xf_handle {
     xf::Dev dev{};
     xf::Shape shape;
     xf::Mixed* mixed = nullptr;
+    xf_io* io = nullptr;
 
     // host bookkeeping
     bool j0_valid = false;
