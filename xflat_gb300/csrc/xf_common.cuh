@@ -93,6 +93,28 @@ __device__ __forceinline__ BeamH beam_offsets(const Dev& d, const double* J, int
     return h;
 }
 
+// Component k of beam_offsets (0: h00 part s (H0 + hm), 1: h01r part s H2,
+// 2: h01i part H3), with the same operations, for lane-parallel per-beam
+// set-up: a warp evaluates one scalar per lane and broadcasts them, instead of
+// every lane evaluating every scalar on the (slow) FP64 pipe.
+template <int GEOM>
+__device__ __forceinline__ double beam_offset_k(const Dev& d, const double* J, int pt, double hm, const BeamIdx& bi,
+                                                int k)
+{
+    const int z = k == 0 ? 0 : (k == 1 ? 2 : 3);
+    const double c = d.geo[geo_idx(0, pt, bi.ang, d.A)];
+    double H;
+    if (GEOM == 0) {
+        H = (J[z] - (J[4 + z] * c)) * d.kappa;
+    } else {
+        const double s = d.geo[geo_idx(1, pt, bi.ang, d.A)];
+        const double cp = d.cosphi[bi.phi], sp = d.sinphi[bi.phi];
+        H = (J[z] - (s * cp * J[4 + z] + s * sp * J[8 + z] + c * J[12 + z])) * d.kappa;
+    }
+    if (k == 0) H = H + hm;
+    return (k < 2 && (bi.p & 1)) ? -H : H;
+}
+
 // L/<E> of particle p without a dynamic index into the kernel parameters
 // (which would copy the array to local memory).
 __device__ __forceinline__ double le_of(const Dev& d, int p)

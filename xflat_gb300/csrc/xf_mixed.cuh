@@ -231,6 +231,36 @@ __device__ __forceinline__ H3f bin_h(const BeamH& b, float hv0, float hv1)
     return h;
 }
 
+// Offset k of the beam Hamiltonian at stage s of phase C: s = 0 the start
+// (J0, point 0), 1 the A1 stage (point 2), 2 the A3 stage (point 1), 3 the B4
+// stage (point 2).  Selected with conditionals so no local array is formed.
+template <int GEOM>
+__device__ __forceinline__ double stage_offset(const Dev& d, const Ctl* ctl, int s, const BeamIdx& bi, int k)
+{
+    const double* J = s == 0 ? ctl->J0 : s == 1 ? ctl->JA1 : s == 2 ? ctl->JA3 : ctl->JB4;
+    const int pt = s == 0 ? 0 : s == 2 ? 1 : 2;
+    const double hm = ctl->hm[pt];
+    return beam_offset_k<GEOM>(d, J, pt, hm, bi, k);
+}
+
+__device__ __forceinline__ H3f bin_hf(const H3f& g, float hv0, float hv1)
+{
+    H3f h;
+    h.h00 = hv0 + g.h00;
+    h.h01r = hv1 + g.h01r;
+    h.h01i = g.h01i;
+    return h;
+}
+
+__device__ __forceinline__ H3f shfl_h3(float v, int first)
+{
+    H3f h;
+    h.h00 = __shfl_sync(kFull, v, first);
+    h.h01r = __shfl_sync(kFull, v, first + 1);
+    h.h01i = __shfl_sync(kFull, v, first + 2);
+    return h;
+}
+
 __device__ __forceinline__ H3f diff_beam(const BeamH& a, const BeamH& b)
 {
     H3f d;
@@ -269,15 +299,19 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     const int myv = lane >> 2;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
-        const BeamH g0 = beam_offsets<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi);
-        const float l1 = (float)geo(d, 3, 1, bi.ang), l0 = (float)geo(d, 3, 0, bi.ang);
+        // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
+        float sv = 0.f;
+        if (lane < 3) sv = (float)beam_offset_k<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi, lane);
+        else if (lane < 5) sv = (float)geo(d, 3, lane - 3, bi.ang);
+        const H3f g0 = shfl_h3(sv, 0);
+        const float l0 = __shfl_sync(kFull, sv, 3), l1 = __shfl_sync(kFull, sv, 4);
         const float* in = p0 + (size_t)b * 4 * epad;
         const float* fvp = d.fvf + bi.p * epad;
         KSum s[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) s[i] = KSum{0.f, 0.f};
         for (int e = lane; e < epad; e += 32) {
-            const H3f h = bin_h(g0, d.hvf[e], d.hvf[epad + e]);
+            const H3f h = bin_hf(g0, d.hvf[e], d.hvf[epad + e]);
             const F4 x = load_f(in, epad, e);
             const KC k0 = kcoef(h, l0);
             KC k1;
@@ -340,13 +374,17 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
-        const BeamH g3 = beam_offsets<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi);
-        const float l1 = (float)geo(d, 3, 1, bi.ang);
+        // lane-parallel set-up: lanes 0-2 the offsets of H3, lane 3 dl1
+        float sv = 0.f;
+        if (lane < 3) sv = (float)beam_offset_k<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi, lane);
+        else if (lane == 3) sv = (float)geo(d, 3, 1, bi.ang);
+        const H3f g3 = shfl_h3(sv, 0);
+        const float l1 = __shfl_sync(kFull, sv, 3);
         const float* in = p0 + (size_t)b * 4 * epad;
         const float* fvp = d.fvf + bi.p * epad;
         KSum s0{0.f, 0.f}, s2{0.f, 0.f}, s3{0.f, 0.f};
         for (int e = lane; e < epad; e += 32) {
-            const H3f h = bin_h(g3, d.hvf[e], d.hvf[epad + e]);
+            const H3f h = bin_hf(g3, d.hvf[e], d.hvf[epad + e]);
             const F4 x = load_f(in, epad, e);
             acc_drho(x, k_apply(kcoef(h, l1), h, x), fvp[e], s0, s2, s3);
         }
@@ -392,23 +430,35 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
-        const BeamH g0 = beam_offsets<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi);
-        const BeamH g1 = beam_offsets<GEOM>(d, ctl->JA1, 2, ctl->hm[2], bi);
-        const BeamH g3 = beam_offsets<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi);
-        const BeamH g4 = beam_offsets<GEOM>(d, ctl->JB4, 2, ctl->hm[2], bi);
-        const H3f d31 = diff_beam(g3, g1), d40 = diff_beam(g4, g0);
-        const double L0 = geo(d, 3, 0, bi.ang), L1 = geo(d, 3, 1, bi.ang), L2 = geo(d, 3, 2, bi.ang);
-        const float l0 = (float)L0, l1 = (float)L1, l2 = (float)L2;
-        const float dl20 = (float)(L2 - L0);
-        const float dl01 = (float)(2.0 * L0 - L1);  // zero in MA
+        // lane-parallel set-up, one scalar per lane: offsets of H0, H1, H3, H4
+        // (lanes 0-11), the differences H3 - H1 and H4 - H0 in FP64 (12-17),
+        // dl0, dl1, dl2, dl2 - dl0 and 2 dl0 - dl1 (18-22)
+        float su = 0.f;  // this lane's scalar
+        if (lane < 18) {
+            const int k = lane % 3;
+            const int sa = lane < 12 ? lane / 3 : (lane < 15 ? 2 : 3);
+            const int sb = lane < 12 ? sa : (lane < 15 ? 1 : 0);
+            const double va = stage_offset<GEOM>(d, ctl, sa, bi, k);
+            const double vb = stage_offset<GEOM>(d, ctl, sb, bi, k);
+            su = (float)(lane < 12 ? va : va - vb);
+        } else if (lane < 23) {
+            const double L0 = geo(d, 3, 0, bi.ang), L1 = geo(d, 3, 1, bi.ang), L2 = geo(d, 3, 2, bi.ang);
+            const int j = lane - 18;
+            // the last, 2 dl0 - dl1, is zero in MA
+            su = (float)(j == 0 ? L0 : j == 1 ? L1 : j == 2 ? L2 : j == 3 ? L2 - L0 : 2.0 * L0 - L1);
+        }
+        const H3f g0 = shfl_h3(su, 0), g1 = shfl_h3(su, 3), g3 = shfl_h3(su, 6), g4 = shfl_h3(su, 9);
+        const H3f d31 = shfl_h3(su, 12), d40 = shfl_h3(su, 15);
+        const float l0 = __shfl_sync(kFull, su, 18), l1 = __shfl_sync(kFull, su, 19), l2 = __shfl_sync(kFull, su, 20);
+        const float dl20 = __shfl_sync(kFull, su, 21), dl01 = __shfl_sync(kFull, su, 22);
         const size_t base = (size_t)b * 4 * epad;
         const float* fvp = d.fvf + bi.p * epad;
         KSum s0{0.f, 0.f}, s2{0.f, 0.f}, s3{0.f, 0.f};
         float err = 0.f;
         for (int e = lane; e < epad; e += 32) {
             const float hv0 = d.hvf[e], hv1 = d.hvf[epad + e];
-            const H3f h0 = bin_h(g0, hv0, hv1), h1 = bin_h(g1, hv0, hv1);
-            const H3f h3 = bin_h(g3, hv0, hv1), h4 = bin_h(g4, hv0, hv1);
+            const H3f h0 = bin_hf(g0, hv0, hv1), h1 = bin_hf(g1, hv0, hv1);
+            const H3f h3 = bin_hf(g3, hv0, hv1), h4 = bin_hf(g4, hv0, hv1);
             const F4 x = load_f(hi0 + base, epad, e);
             const KC k0 = kcoef(h0, l0), k4 = kcoef(h4, l2), k3 = kcoef(h3, l1);
             const F4 d3 = k_apply(k0, h0, x);
