@@ -42,7 +42,10 @@ enum {
     XF_EUNSUPPORTED = 7  /* option not supported for this geometry/precision */
 };
 
-enum { XF_GEOM_MA = 0, XF_GEOM_MAA = 1 };
+/* MA and MAA: bulb model with polar (and azimuthal) angle bins; SA: the
+ * single-angle bulb model (src/Phy_SA.cpp), one beam per particle, Abins and
+ * Pbins ignored. */
+enum { XF_GEOM_MA = 0, XF_GEOM_MAA = 1, XF_GEOM_SA = 2 };
 enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
 
 /* Run configuration.  Fields carry the reference's Util:: values in the same
@@ -51,7 +54,7 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
  * Keys missing from a config file keep the xf_config_default() value (the
  * reference leaves them uninitialized). */
 typedef struct xf_config {
-    int geometry;        /* XF_GEOM_*  (extension key "geometry= MA|MAA") */
+    int geometry;        /* XF_GEOM_*  (extension key "geometry= MA|MAA|SA") */
     int precision;       /* XF_PREC_*  (extension key "precision= fp64|mixed") */
     int abins, pbins, ebins, flvs;
     int has_matter;      /* hasMatter= */
@@ -239,8 +242,8 @@ int xf_snapshot_read(const char* path, long rec, double* r, double* dr, double* 
 /* ---------------------------------------------------------------- batch */
 /* Many independent simulations with per-instance adaptive steps, advanced
  * together by the same phase kernels (one launch per phase covers every
- * instance), captured in CUDA graphs.  All configs must share geometry (MA)
- * and precision. */
+ * instance), captured in CUDA graphs.  Configs may be MA or SA (they share
+ * the MA-shaped kernels) and must share precision. */
 typedef struct xf_batch xf_batch;
 int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out);
 int xf_batch_destroy(xf_batch* b);

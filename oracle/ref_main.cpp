@@ -10,7 +10,7 @@
 // and then writes the accepted-step log, the final state and (optionally) the
 // intermediate stage buffers and the per-step tables to raw files.
 //
-// usage: xflat_ref_{ma,maa} <config> [--state-in F] [--noise SEED AMP]
+// usage: xflat_ref_{ma,maa,sa} <config> [--state-in F] [--noise SEED AMP]
 //            [--state-out F] [--log F] [--stages PREFIX] [--probe F]
 //
 // File formats: raw little-endian float64.  States use the reference's NetCDF
@@ -55,6 +55,12 @@ extern double* sin_tetbins;
 extern double* dcos_tetbins;
 extern double* delta_l;
 extern int tetbins;
+}
+#elif defined(SA)
+namespace phy_sa {
+extern double* L_E;
+extern double* rarr;
+extern double* delta_l;
 }
 #else
 namespace phy_ma {
@@ -204,6 +210,12 @@ int main(int argc, char* argv[])
         probe_rec(f, "dcos", P::dcos_tetbins, 3 * P::tetbins);
         probe_rec(f, "dl", P::delta_l, 3 * P::tetbins);
         const int nh = len;  // (theta*phi) * 4 doubles = len
+#elif defined(SA)
+        namespace P = nbgrp::phy_sa;
+        probe_rec(f, "LE", P::L_E, 4);
+        probe_rec(f, "rpt", P::rarr, 3);
+        probe_rec(f, "dl", P::delta_l, 3);
+        const int nh = 4;  // one 4-vector shared by the four particle beams
 #else
         namespace P = nbgrp::phy_ma;
         probe_rec(f, "LE", P::L_E, 4);

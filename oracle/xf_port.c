@@ -1,7 +1,7 @@
 /*
  * Oracle (test infrastructure only; never linked into the product).
  *
- * Plain-C restatement of the reference's hot path (bulb-model MA/MAA geometry,
+ * Plain-C restatement of the reference's hot path (bulb-model MA/MAA and single-angle SA geometry,
  * the NBeam per-bin SU(2) kernels and the adaptive three-point stepper).  The
  * loop structure (OpenMP over angle bins, omp simd over energy bins) and the
  * floating-point operation order follow the reference line by line, so the
@@ -44,6 +44,7 @@ struct xfp_sim {
     int tet, pb, nbeams, ne;
     double *Cos2R, *dCos2R, *SinR, *sinphi, *cosphi, dPhi;
     double *cosb, *sinb, *dcosb, *dl; /* [3][tet] */
+    double rpt[3];                     /* SA: radius of each stage point (src/Phy_SA.cpp:121-124) */
     double integ_coef, LE[4];
     /* matt (src/Matt.cpp:22-29) */
     double mat_coeff, nbfar_coeff;
@@ -106,7 +107,11 @@ static void set_key(xfp_sim* s, const char* k, const char* v)
     else if (!strcmp(k, "eta_vt=")) s->eta[2] = d;
     else if (!strcmp(k, "eta_v_t=")) s->eta[3] = d;
     /* extension keys (skipped by the reference parser) */
-    else if (!strcmp(k, "geometry=")) s->geom = (v[0] == 'M' && v[1] == 'A' && v[2] == 'A') ? 1 : 0;
+    else if (!strcmp(k, "geometry=")) {
+        if ((v[0] == 'M' || v[0] == 'm') && (v[1] == 'A' || v[1] == 'a') && (v[2] == 'A' || v[2] == 'a')) s->geom = 1;
+        else if ((v[0] == 'S' || v[0] == 's') && (v[1] == 'A' || v[1] == 'a')) s->geom = 2;
+        else s->geom = 0;
+    }
     else if (!strcmp(k, "seed=")) s->seed = strtoull(v, NULL, 10);
     else if (!strcmp(k, "noise_amp=")) s->noise_amp = d;
 }
@@ -231,10 +236,29 @@ static void init_angles(xfp_sim* s)
     }
 }
 
-/* src/Phy_MA.cpp:172-196, src/Phy_MAA.cpp:194-210 */
+/* SA dilution factor D(r) = (1 - sqrt(1 - (Rv/r)^2))^2 / 2, src/Phy_SA.cpp:250-256 */
+static double sa_D(double Rv, double r)
+{
+    double R = Rv / r;
+    double tm = 1. - sqrt(1. - (R * R));
+    return 0.5 * (tm * tm);
+}
+
+/* src/Phy_MA.cpp:172-196, src/Phy_MAA.cpp:194-210; SA keeps only the radius
+ * (src/Phy_SA.cpp:121-124).  For SA the tables report cos = sin = 0 and the
+ * dilution factor D(r) in the weight slot, the form in which an MA-shaped
+ * moment H = kappa (J0 - cos J1) with J0 = sum w N reduces to SA's
+ * kappa D(r) sum N. */
 static void calc_angle_bins(xfp_sim* s, double r, int step)
 {
     const int T = s->tet;
+    if (s->geom == 2) {
+        s->rpt[step] = r;
+        s->cosb[step] = 0.;
+        s->sinb[step] = 0.;
+        s->dcosb[step] = sa_D(s->Rv, r);
+        return;
+    }
     double ra = s->Rv / r;
     double r2 = ra * ra;
 #pragma omp parallel for
@@ -250,6 +274,10 @@ static void calc_angle_bins(xfp_sim* s, double r, int step)
 static void calc_delta_ls(xfp_sim* s, double dr, int cur, int sp, int ep)
 {
     const int T = s->tet;
+    if (s->geom == 2) { /* src/Phy_SA.cpp:144-147 */
+        s->dl[cur] = dr;
+        return;
+    }
 #pragma omp parallel for
     for (int ang = 0; ang < T; ++ang) {
         if (s->geom == 1)
@@ -510,9 +538,22 @@ static void calc_hvv_maa(xfp_sim* s, const double* hs, int step, double* hvv)
         }
 }
 
+/* SA: src/Phy_SA.cpp:259-281 */
+static void calc_hvv_sa(xfp_sim* s, const double* hs, int step, double* hvv)
+{
+    for (int z = 0; z < 4; ++z) hvv[z] = 0.;
+    for (int n = 0; n < s->Flvs; ++n) {
+        int neu = n << 1, aneu = neu + 1;
+        upd_nu_coef(&hs[4 * neu], &hs[4 * aneu], s->LE[neu], s->LE[aneu], hvv);
+    }
+    double coeff = s->integ_coef * sa_D(s->Rv, s->rpt[step]);
+    for (int z = 0; z < 4; ++z) hvv[z] *= coeff;
+}
+
 static void calc_hvv(xfp_sim* s, const double* hs, int step, double* hvv)
 {
-    if (s->geom == 1) calc_hvv_maa(s, hs, step, hvv);
+    if (s->geom == 2) calc_hvv_sa(s, hs, step, hvv);
+    else if (s->geom == 1) calc_hvv_maa(s, hs, step, hvv);
     else calc_hvv_ma(s, hs, step, hvv);
 }
 
@@ -554,7 +595,8 @@ xfp_sim* xfp_create(const char* path)
         return NULL;
     }
     if (s->geom == 0) s->Pbins = s->Pbins > 0 ? s->Pbins : 1;
-    s->tet = s->Abins;
+    /* SA: one beam per particle whatever Abins says (src/Phy_SA.cpp:150-184) */
+    s->tet = (s->geom == 2) ? 1 : s->Abins;
     s->pb = (s->geom == 1) ? s->Pbins : 1;
     s->ne = s->Ebins;
     s->nbeams = s->tet * s->pb * 2 * s->Flvs;
@@ -563,7 +605,7 @@ xfp_sim* xfp_create(const char* path)
     if (s->geom == 1)
         s->integ_coef = ((U_SQRT2 * U_GF) / (4. * U_PI * U_PI * s->Rv * s->Rv)) * s->dPhi;
     else
-        s->integ_coef = (U_SQRT2 * U_GF) / (2. * U_PI * s->Rv * s->Rv);
+        s->integ_coef = (U_SQRT2 * U_GF) / (2. * U_PI * s->Rv * s->Rv); /* MA :271, SA src/Phy_SA.cpp:167-168 */
     for (int i = 0; i < 4; ++i) s->LE[i] = s->Lv[i] / s->Ev[i];
     matt_init(s);
     const size_t T3 = (size_t)3 * s->tet * sizeof(double);

@@ -2,7 +2,7 @@
  * Oracle (test infrastructure only; never linked into the product).
  *
  * Plain-C restatement of the reference's per-radius-step hot path for the
- * bulb-model MA and MAA geometries, used as the checker for the CUDA path and
+ * bulb-model MA, MAA and single-angle SA geometries, used as the checker for the CUDA path and
  * as the timed CPU baseline where the reference itself cannot be compiled.
  * Every function cites the reference file:line it restates.  The restatement is
  * pinned against outputs of the reference itself (oracle/_ref, built from the
@@ -25,7 +25,7 @@ typedef struct xfp_sim xfp_sim;
 xfp_sim* xfp_create(const char* config_path);
 void xfp_destroy(xfp_sim* s);
 
-int xfp_geometry(const xfp_sim* s);   /* 0 = MA, 1 = MAA */
+int xfp_geometry(const xfp_sim* s);   /* 0 = MA, 1 = MAA, 2 = SA */
 int xfp_nbeams(const xfp_sim* s);     /* theta * phi * 4 */
 int xfp_ebins(const xfp_sim* s);
 int xfp_abins(const xfp_sim* s);

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
 The reference's own hot-path sources are compiled by ``oracle/Makefile`` (target
-``ref``) into ``oracle/_ref/xflat_ref_{ma,maa}``; this script runs those binaries
+``ref``) into ``oracle/_ref/xflat_ref_{ma,maa,sa}``; this script runs those binaries
 on small configurations derived from the workload configs and stores what they
 print into compressed ``.npz`` files:
 
@@ -14,7 +14,7 @@ print into compressed ``.npz`` files:
 * ``probe_*`` energy tables, matter terms, angle tables and the Hamiltonian at
              the three stage points on the initial state (src/NBeam.cpp:138-209,
              src/Matt.cpp:58-64, src/Phy_MA.cpp:172-227/455-474,
-             src/Phy_MAA.cpp:194-241/571-621);
+             src/Phy_MAA.cpp:194-241/571-621, src/Phy_SA.cpp:121-147/259-281);
 * ``stage_*`` every stage buffer after one forced iteration (src/Nmr.cpp:153-206).
 
 Run it from the repository root, in a checkout that has the reference sources:
@@ -54,7 +54,12 @@ CASES = [
      "replay probe stages"),
     ("ma_c1shape_probe", "config1_ma.txt", dict(Ts=0), 1e-7, "probe"),
     ("maa_c3shape_probe", "config3_maa.txt", dict(Ts=0), 1e-6, "probe"),
+    ("sa_r10", "sa_bulb.txt", dict(Ebins=64, R0=10, dr=1e-3, Ts=600), 1e-7, "replay probe stages"),
+    ("sa_r60", "sa_bulb.txt", dict(R0=60, dr=1e-3, Ts=1500), 1e-7, "replay probe"),
+    ("sa_ragged", "sa_bulb.txt", dict(Abins=7, Ebins=37, R0=25, dr=1e-5, Ts=400, dm2="3E-3"), 1e-7,
+     "replay probe stages"),
 ]
+EXES = {"MA": "xflat_ref_ma", "MAA": "xflat_ref_maa", "SA": "xflat_ref_sa"}
 SEED = 1
 
 
@@ -83,8 +88,7 @@ def run_case(name, base, overrides, amp, outputs, refdir, tmp):
     text = derive_config(open(os.path.join(CONFIGS, base)).read(), overrides)
     cfg_path = os.path.join(tmp, name + ".txt")
     open(cfg_path, "w").write(text)
-    exe = os.path.join(refdir, "xflat_ref_maa" if "MAA" in re.search(r"^geometry=\s*(\S+)", text, re.M).group(1)
-                       else "xflat_ref_ma")
+    exe = os.path.join(refdir, EXES[re.search(r"^geometry=\s*(\S+)", text, re.M).group(1).upper()])
     pre = os.path.join(tmp, name)
     cmd = [exe, cfg_path, "--noise", str(SEED), repr(amp), "--state-out", pre + "_final.bin", "--log", pre + "_log.bin"]
     if "probe" in outputs:

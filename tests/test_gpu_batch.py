@@ -1,5 +1,6 @@
-"""Batched path: independent MA instances of uneven shapes advanced by shared
-launches with per-instance step control, against the same instances run alone."""
+"""Batched path: independent MA (and SA) instances of uneven shapes advanced by
+shared launches with per-instance step control, against the same instances run
+alone."""
 import numpy as np
 import pytest
 
@@ -58,3 +59,17 @@ def test_batch_rejects_mixed_geometry():
     texts[1] = texts[1].replace("geometry= MA", "geometry= MAA")
     with pytest.raises(xg.XflatError):
         xg.Batch([xg.Config.from_text(t) for t in texts])
+
+
+def test_batch_with_sa_instances():
+    """SA instances share the MA-shaped kernels, so they batch with MA ones."""
+    texts = _small_sweep(n=3)
+    texts.append(derive("sa_bulb.txt", Ebins=48, R0=10, dr="1e-3"))
+    texts.append(derive("sa_bulb.txt", Ebins=5, R0=60, dr="1e-3"))
+    b = xg.Batch([xg.Config.from_text(t) for t in texts])
+    out = b.run(max_iters=60)
+    for i in (3, 4):
+        s = xg.Simulation(xg.Config.from_text(texts[i]))
+        o = s.evolutionLoop(max_iters=60, device_control=True)
+        assert (o["iterations"], o["accepted"]) == (out["iterations"][i], out["accepted"][i])
+        assert pol_rel_err(b.get_state(i), s.get_state(0)) <= 1e-10

@@ -104,3 +104,14 @@ def test_mixed_rejects_unkept_buffers():
     b = xg.Simulation(xg.Config.from_text(derive("config0_ma.txt", Abins=4, Ebins=8, precision="mixed")))
     with pytest.raises(xg.XflatError):
         b.get_state(1)
+
+
+def test_sa_free_running_window_vs_fp64():
+    text = derive("sa_bulb.txt", R0=10, dr="1e-3")
+    a, b = _pair(text)
+    oa = a.evolutionLoop(max_iters=600, device_control=True)
+    ob = b.evolutionLoop(max_iters=600, device_control=True)
+    assert abs(oa["accepted"] - ob["accepted"]) <= 2
+    if oa["accepted"] == ob["accepted"]:
+        d = np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0))))
+        assert d <= 1e-5, d

@@ -27,12 +27,20 @@ def test_tables_angles_and_hamiltonian_vs_reference(name):
     np.testing.assert_allclose(t["hvac"], g["probe_hvac"], rtol=1e-14, atol=0)
     r, dr = key(g["config"], "R0"), key(g["config"], "dr")
     c, s, d, l = sim.calcAngleBins(r, dr)
-    # device sqrt and division are correctly rounded; contraction differs (see oracle tests)
-    np.testing.assert_allclose(c.reshape(-1), g["probe_cos"], rtol=2e-13, atol=0)
-    np.testing.assert_allclose(d.reshape(-1), g["probe_dcos"], rtol=2e-13, atol=0)
-    np.testing.assert_allclose(l.reshape(-1), g["probe_dl"], rtol=2e-13, atol=0)
-    if "probe_sin" in g:
-        np.testing.assert_allclose(s.reshape(-1), g["probe_sin"], rtol=2e-13, atol=0)
+    if "probe_rpt" in g:
+        # SA: dl = dr/2, dr, dr/2 exactly; the weight slot holds D(r) at the
+        # reference's stage radii (src/Phy_SA.cpp:121-147, 250-256)
+        np.testing.assert_array_equal(l.reshape(-1), g["probe_dl"])
+        R = key(g["config"], "Rv") / g["probe_rpt"]
+        np.testing.assert_allclose(d.reshape(-1), .5 * (1. - np.sqrt(1. - R * R)) ** 2, rtol=1e-14, atol=0)
+        assert not c.any() and not s.any()
+    else:
+        # device sqrt and division are correctly rounded; contraction differs (see oracle tests)
+        np.testing.assert_allclose(c.reshape(-1), g["probe_cos"], rtol=2e-13, atol=0)
+        np.testing.assert_allclose(d.reshape(-1), g["probe_dcos"], rtol=2e-13, atol=0)
+        np.testing.assert_allclose(l.reshape(-1), g["probe_dl"], rtol=2e-13, atol=0)
+        if "probe_sin" in g:
+            np.testing.assert_allclose(s.reshape(-1), g["probe_sin"], rtol=2e-13, atol=0)
     sim.set_noise(g["meta"]["seed"], g["meta"]["noise_amp"])
     for pt in range(3):
         h = sim.calc_Hvv(0, pt, r, dr).reshape(-1)
@@ -211,3 +219,30 @@ def test_survival_probabilities():
     sv = s.survival()
     ref = np.einsum("bpe,pe->bp", (psi[:, 0] ** 2 + psi[:, 1] ** 2).reshape(8, 4, 16), fv[[0, 1, 0, 1]])
     np.testing.assert_allclose(sv, ref, rtol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["sa_r10", "sa_r60"])
+def test_sa_free_running_vs_reference(name):
+    """Single-angle geometry on the MA-shaped kernels, device-controlled loop:
+    the reference's own accept/reject sequence (src/Phy_SA.cpp + src/Nmr.cpp),
+    dr to the precision the step-error cancellation allows."""
+    g = golden(name)
+    sim = _sim(g["config"])
+    assert (sim.nbeams, sim.abins, sim.pbins) == (4, 1, 1)
+    sim.set_noise(g["meta"]["seed"], g["meta"]["noise_amp"])
+    out = sim.evolutionLoop(max_iters=g["meta"]["summary"]["iterations"], log_cap=100000, device_control=True)
+    log = g["log"]
+    assert out["accepted"] == len(log)
+    np.testing.assert_array_equal(out["log"][:, 0], log[:, 0])
+    np.testing.assert_allclose(out["log"][:, 2], log[:, 2], rtol=1e-5)
+
+
+def test_sa_ignores_abins():
+    """SA has one trajectory whatever Abins says (src/Phy_SA.cpp:150-184)."""
+    a = _sim(derive("sa_bulb.txt", Abins=1, Ebins=40))
+    b = _sim(derive("sa_bulb.txt", Abins=300, Ebins=40))
+    assert a.nbeams == b.nbeams == 4
+    for s in (a, b):
+        s.set_noise(1, 1e-7)
+        s.evolutionLoop(max_iters=50)
+    assert np.array_equal(a.get_state(0), b.get_state(0))

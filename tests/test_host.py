@@ -37,6 +37,8 @@ def test_config_units_and_keys():
     assert c3.geometry == xg.XF_GEOM_MAA and c3.pbins == 64
     c2 = xg.Parser(os.path.join(CONFIGS, "config2_ma_mixed.txt"))
     assert c2.precision == xg.XF_PREC_MIXED
+    sa = xg.Parser(os.path.join(CONFIGS, "sa_bulb.txt"))
+    assert sa.geometry == xg.XF_GEOM_SA and sa.ebins == 512
 
 
 def test_config_reference_syntax():
@@ -85,11 +87,13 @@ def test_matter_profile_is_the_baseline_lambda():
         assert abs(2 * o.value / (1e3 * (10. / r) ** 3) - 1) < 1e-5
 
 
-@pytest.mark.parametrize("geom,a,p,e", [("config0_ma.txt", 13, 1, 21), ("config3_maa.txt", 5, 3, 9)])
+@pytest.mark.parametrize("geom,a,p,e", [("config0_ma.txt", 13, 1, 21), ("config3_maa.txt", 5, 3, 9),
+                                        ("sa_bulb.txt", 6, 1, 11)])
 def test_host_initial_state_matches_numpy_and_oracle(geom, a, p, e):
     text = derive(geom, Abins=a, Pbins=p, Ebins=e)
     c = xg.Config.from_text(text)
-    nb = a * (p if c.geometry == 1 else 1) * 4
+    # SA: one trajectory whatever Abins says
+    nb = (1 if c.geometry == xg.XF_GEOM_SA else a) * (p if c.geometry == xg.XF_GEOM_MAA else 1) * 4
     psi = np.empty(nb * 4 * e)
     assert _abi.load().xf_host_initial_state(ctypes.byref(c.raw), 7, 1e-6, psi.ctypes.data_as(_abi.c_double_p)) == 0
     ref = noise_state(nb, e, 7, 1e-6)

@@ -23,6 +23,8 @@ def _write(path, cfg, psi, r, dr):
 @pytest.mark.parametrize("base,over,shape", [
     ("config0_ma.txt", dict(Abins=5, Ebins=7), (5, 4, 4, 7)),
     ("config3_maa.txt", dict(Abins=3, Pbins=2, Ebins=6), (3, 2, 4, 4, 6)),
+    # SA: no angle dimension (src/Phy_SA.cpp:67-96), Abins ignored
+    ("sa_bulb.txt", dict(Abins=9, Ebins=5), (4, 4, 5)),
 ])
 def test_snapshot_file_matches_reference_layout(tmp_path, base, over, shape):
     cfg = xg.Config.from_text(derive(base, **over))
@@ -34,7 +36,8 @@ def test_snapshot_file_matches_reference_layout(tmp_path, base, over, shape):
     path = tmp_path / "xSnapshot0_0_.nc"
     assert _write(path, cfg, np.ascontiguousarray(psi), r, dr) == 0
     with scipy_io.netcdf_file(str(path), "r", mmap=False) as f:
-        dims = ["r", "theta"] + (["phi"] if len(shape) == 5 else []) + ["prtcl", "comp", "ebin"]
+        dims = ["r"] + (["theta"] if len(shape) >= 4 else []) + (["phi"] if len(shape) == 5 else []) + \
+            ["prtcl", "comp", "ebin"]
         assert list(f.variables["psi"].dimensions) == dims
         assert f.variables["psi"].shape == (nrec,) + shape
         np.testing.assert_array_equal(f.variables["psi"][:], psi)

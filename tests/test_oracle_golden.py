@@ -46,9 +46,18 @@ def test_angle_tables_and_hamiltonian(name):
     p = _port(g)
     r, dr = key(g["config"], "R0"), key(g["config"], "dr")
     c, s, d, l = p.probe(r, dr)
-    np.testing.assert_allclose(c.reshape(-1), g["probe_cos"], rtol=2e-13, atol=0)  # cancellation in 1 - r2 (1 - u) near the limb: rel. err ~ ulp / (2 cos^2)
-    np.testing.assert_allclose(d.reshape(-1), g["probe_dcos"], rtol=2e-13, atol=0)
-    np.testing.assert_allclose(l.reshape(-1), g["probe_dl"], rtol=2e-13, atol=0)
+    if "probe_rpt" in g:
+        # SA keeps the stage radii and dl = dr/2, dr, dr/2 (src/Phy_SA.cpp:121-147);
+        # the port reports the dilution factor D(r) in the weight slot
+        assert np.array_equal(g["probe_rpt"], [r, r + .5 * dr, r + dr])
+        np.testing.assert_array_equal(l.reshape(-1), g["probe_dl"])
+        R = key(g["config"], "Rv") / g["probe_rpt"]
+        np.testing.assert_allclose(d.reshape(-1), .5 * (1. - np.sqrt(1. - R * R)) ** 2, rtol=1e-14, atol=0)
+        assert not c.any() and not s.any()
+    else:
+        np.testing.assert_allclose(c.reshape(-1), g["probe_cos"], rtol=2e-13, atol=0)  # cancellation in 1 - r2 (1 - u) near the limb: rel. err ~ ulp / (2 cos^2)
+        np.testing.assert_allclose(d.reshape(-1), g["probe_dcos"], rtol=2e-13, atol=0)
+        np.testing.assert_allclose(l.reshape(-1), g["probe_dl"], rtol=2e-13, atol=0)
     if "probe_sin" in g:
         np.testing.assert_allclose(s.reshape(-1), g["probe_sin"], rtol=1e-15, atol=0)
     p.noise(g["meta"]["seed"], g["meta"]["noise_amp"])
@@ -87,7 +96,7 @@ def test_replay_of_reference_step_sequence(name):
     assert pol_rel_err(p.get_state(0), final) <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["ma_small_r10", "ma_small_r50", "maa_small_r10", "ma_nomatter"])
+@pytest.mark.parametrize("name", ["ma_small_r10", "ma_small_r50", "maa_small_r10", "ma_nomatter", "sa_r10", "sa_r60"])
 def test_free_running_loop_matches_reference(name):
     """The free-running loop takes the same accept/reject decisions; dr agrees
     to the precision the step-error cancellation allows."""

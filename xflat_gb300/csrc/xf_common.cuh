@@ -333,6 +333,24 @@ __device__ inline void geometry_body(const Dev& d, int ang)
         }
     }
     if (ang >= d.A) return;
+    if (d.sa) {
+        // SA (src/Phy_SA.cpp:121-147, 250-256): no angular dependence, dl =
+        // dr/2, dr, dr/2, and H = kappa D(r) N.  Stored in the MA layout as
+        // cos = 0 and weight D(r), so the MA moment J0 = sum_b w N_b gives
+        // H = kappa (J0 - cos J1) = kappa D(r) N.
+#pragma unroll
+        for (int pt = 0; pt < 3; ++pt) {
+            const double R = d.Rv / rp[pt];
+            const double tm = 1. - sqrt(1. - (R * R));
+            d.geo[geo_idx(0, pt, ang, d.A)] = 0.;
+            d.geo[geo_idx(1, pt, ang, d.A)] = 0.;
+            d.geo[geo_idx(2, pt, ang, d.A)] = .5 * (tm * tm);
+        }
+        d.geo[geo_idx(3, 0, ang, d.A)] = dr2;
+        d.geo[geo_idx(3, 1, ang, d.A)] = dr;
+        d.geo[geo_idx(3, 2, ang, d.A)] = dr2;
+        return;
+    }
     double c[3];
 #pragma unroll
     for (int pt = 0; pt < 3; ++pt) {

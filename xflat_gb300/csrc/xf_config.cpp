@@ -122,6 +122,7 @@ int parse_stream(std::istream& in, xf_config* c)
             ss >> s;
             if (s == "MAA" || s == "maa") c->geometry = XF_GEOM_MAA;
             else if (s == "MA" || s == "ma") c->geometry = XF_GEOM_MA;
+            else if (s == "SA" || s == "sa") c->geometry = XF_GEOM_SA;
             else return XF_EINVAL;
         }
         else if (k == "precision=") {

@@ -54,7 +54,8 @@ struct Ctl {
 
 // Kernel parameters (passed by value).
 struct Dev {
-    int geom;             // 0 MA, 1 MAA
+    int geom;             // kernel family: 0 MA-shaped moments (MA and SA), 1 MAA
+    int sa;               // SA geometry table (single angle, dilution factor D(r))
     int nbeams, A, P, ne, epad;
     const double* fv;     // [4][epad]
     const double* hvac;   // [2][epad]: h00 part, then h01 real part

@@ -41,14 +41,19 @@ constexpr int kDefaultItersPerLaunch = 16;
 
 int check_config(const xf_config& c, std::string& why)
 {
-    if (c.geometry != XF_GEOM_MA && c.geometry != XF_GEOM_MAA) { why = "geometry must be MA or MAA"; return XF_EINVAL; }
+    if (c.geometry != XF_GEOM_MA && c.geometry != XF_GEOM_MAA && c.geometry != XF_GEOM_SA) {
+        why = "geometry must be MA, MAA or SA";
+        return XF_EINVAL;
+    }
     if (c.precision != XF_PREC_FP64 && c.precision != XF_PREC_MIXED) { why = "precision must be fp64 or mixed"; return XF_EINVAL; }
     if (c.flvs != 2) { why = "only two flavors are supported (Flvs= 2), as by the MA/MAA modules"; return XF_EUNSUPPORTED; }
-    if (c.abins <= 0 || c.ebins <= 0) { why = "Abins and Ebins must be positive"; return XF_EINVAL; }
+    if ((c.geometry != XF_GEOM_SA && c.abins <= 0) || c.ebins <= 0) { why = "Abins and Ebins must be positive"; return XF_EINVAL; }
     if (c.geometry == XF_GEOM_MAA && c.pbins <= 0) { why = "Pbins must be positive for MAA"; return XF_EINVAL; }
     if (c.E1 <= c.E0) { why = "E1 must exceed E0"; return XF_EINVAL; }
     if (c.Rv <= 0.) { why = "Rv must be positive"; return XF_EINVAL; }
-    const double nb = (double)c.abins * (c.geometry == XF_GEOM_MAA ? c.pbins : 1) * 4.;
+    int A, P;
+    xf::beam_dims(c, A, P);
+    const double nb = (double)A * P * 4.;
     if (nb > 2147483647.0 / 4) { why = "too many beams"; return XF_EINVAL; }
     return XF_OK;
 }
@@ -88,8 +93,7 @@ int xf_handle::init(const xf_config& c)
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(XF_ECUDA, "no usable GPU");
     XF_CUDA(this, cudaGetDevice(&device));
     xf::build_tables(cfg, tab);
-    A = cfg.abins;
-    P = cfg.geometry == XF_GEOM_MAA ? cfg.pbins : 1;
+    xf::beam_dims(cfg, A, P);
     ne = cfg.ebins;
     epad = (ne + 31) / 32 * 32;
     nbeams = A * P * 4;
@@ -126,7 +130,8 @@ int xf_handle::init(const xf_config& c)
     std::memset(h_ctl, 0, sizeof(Ctl));
 
     dev = Dev{};
-    dev.geom = cfg.geometry;
+    dev.geom = cfg.geometry == XF_GEOM_MAA ? 1 : 0;
+    dev.sa = cfg.geometry == XF_GEOM_SA;
     dev.nbeams = nbeams;
     dev.A = A;
     dev.P = P;

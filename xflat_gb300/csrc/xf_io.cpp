@@ -11,6 +11,7 @@
 
 #include "xf_engine.h"
 #include "xf_netcdf.h"
+#include "xf_physics.h"
 #include "xflat_gpu.h"
 
 struct xf_io {
@@ -36,16 +37,20 @@ std::string file_name(const xf_config& c, const char* kind, int ctr)
     return std::string(c.file_prefix) + kind + std::to_string(ctr) + "_0_.nc";
 }
 
-// Dimensions, variables and attributes of the Snapshot file (src/IO_f.cpp:116-144).
+// Dimensions, variables and attributes of the Snapshot file (src/IO_f.cpp:116-144);
+// the dimensions are the module's getDimInfo/countDim: MA r, theta, prtcl,
+// comp, ebin (src/Phy_MA.cpp), MAA adds phi (src/Phy_MAA.cpp), SA has no
+// angle (src/Phy_SA.cpp:67-96).
 void snapshot_schema(const xf_config& c, std::vector<xf::nc::Dim>& dims, std::vector<xf::nc::Var>& vars)
 {
     using xf::nc::Attr;
     using xf::nc::Dim;
     using xf::nc::Var;
-    const int P = c.geometry == XF_GEOM_MAA ? c.pbins : 1;
+    int A, P;
+    xf::beam_dims(c, A, P);
     dims.clear();
     dims.push_back(Dim{"r", 0});
-    dims.push_back(Dim{"theta", (uint64_t)c.abins});
+    if (c.geometry != XF_GEOM_SA) dims.push_back(Dim{"theta", (uint64_t)A});
     if (c.geometry == XF_GEOM_MAA) dims.push_back(Dim{"phi", (uint64_t)P});
     dims.push_back(Dim{"prtcl", 4});
     dims.push_back(Dim{"comp", 4});
@@ -191,13 +196,16 @@ int xf_dump(xf_handle* h, long it, double r, double dr)
 int xf_snapshot_write(const char* path, const xf_config* c, long nrec, const double* r, const double* dr,
                       const double* psi)
 {
-    if (!path || !c || nrec < 0 || (nrec > 0 && (!r || !dr || !psi)) || c->abins <= 0 || c->ebins <= 0) return XF_EINVAL;
+    int A = 0, P = 0;
+    if (c) xf::beam_dims(*c, A, P);
+    if (!path || !c || nrec < 0 || (nrec > 0 && (!r || !dr || !psi)) || A <= 0 || P <= 0 || c->ebins <= 0)
+        return XF_EINVAL;
     std::vector<xf::nc::Dim> dims;
     std::vector<xf::nc::Var> vars;
     snapshot_schema(*c, dims, vars);
     xf::nc::Writer w;
     if (!w.create(path, dims, vars)) return XF_EIO;
-    const size_t n = (size_t)c->abins * (c->geometry == XF_GEOM_MAA ? c->pbins : 1) * 4 * 4 * c->ebins;
+    const size_t n = (size_t)A * P * 4 * 4 * c->ebins;
     for (long i = 0; i < nrec; ++i)
         if (!w.append({&r[i], &dr[i], psi + (size_t)i * n})) return XF_EIO;
     w.close();

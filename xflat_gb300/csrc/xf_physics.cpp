@@ -64,8 +64,11 @@ void build_tables(const xf_config& c, Tables& t)
 
     // Polar grid uniform in sin^2(theta_R): the reference accumulates the bin
     // centres by repeated subtraction, which is reproduced exactly here because
-    // the angle tables at radius r are built from these values.
-    const int A = c.abins;
+    // the angle tables at radius r are built from these values.  SA has one
+    // trajectory and does not read them; a one-bin grid keeps the sizes
+    // consistent with beam_dims().
+    int A, P_;
+    beam_dims(c, A, P_);
     t.cos2R.assign(A, 0.);
     t.dcos2R.assign(A, 0.);
     t.sinR.assign(A, 0.);
@@ -97,7 +100,7 @@ void build_tables(const xf_config& c, Tables& t)
         // src/Phy_MAA.cpp:297-298
         t.integ_coef = ((kSqrt2 * kGF) / (4. * kPi * kPi * c.Rv * c.Rv)) * dphi;
     } else {
-        // src/Phy_MA.cpp:271-272
+        // src/Phy_MA.cpp:271-272; SA the same (src/Phy_SA.cpp:167-168)
         t.integ_coef = (kSqrt2 * kGF) / (2. * kPi * c.Rv * c.Rv);
     }
 
@@ -164,7 +167,7 @@ void initial_state(int nbeams, int ne, uint64_t seed, double amp, std::vector<do
 
 extern "C" int xf_host_tables(const xf_config* c, double* fv, double* hvac, double* LE, double* Ev)
 {
-    if (!c || c->ebins <= 0 || c->abins <= 0) return XF_EINVAL;
+    if (!c || c->ebins <= 0 || (c->geometry != XF_GEOM_SA && c->abins <= 0)) return XF_EINVAL;
     xf::Tables t;
     xf::build_tables(*c, t);
     if (fv) std::copy(t.fv.begin(), t.fv.end(), fv);
@@ -176,7 +179,7 @@ extern "C" int xf_host_tables(const xf_config* c, double* fv, double* hvac, doub
 
 extern "C" int xf_host_matter(const xf_config* c, double r, double* hm)
 {
-    if (!c || !hm || c->ebins <= 0 || c->abins <= 0) return XF_EINVAL;
+    if (!c || !hm || c->ebins <= 0 || (c->geometry != XF_GEOM_SA && c->abins <= 0)) return XF_EINVAL;
     xf::Tables t;
     xf::build_tables(*c, t);
     *hm = xf::matter_hm(*c, t, r);
@@ -185,10 +188,11 @@ extern "C" int xf_host_matter(const xf_config* c, double r, double* hm)
 
 extern "C" int xf_host_initial_state(const xf_config* c, uint64_t seed, double amp, double* psi)
 {
-    if (!c || !psi || c->ebins <= 0 || c->abins <= 0) return XF_EINVAL;
-    const int P = c->geometry == XF_GEOM_MAA ? c->pbins : 1;
+    if (!c || !psi || c->ebins <= 0 || (c->geometry != XF_GEOM_SA && c->abins <= 0)) return XF_EINVAL;
+    int A, P;
+    xf::beam_dims(*c, A, P);
     std::vector<double> v;
-    xf::initial_state(c->abins * P * 4, c->ebins, seed, amp, v);
+    xf::initial_state(A * P * 4, c->ebins, seed, amp, v);
     std::copy(v.begin(), v.end(), psi);
     return XF_OK;
 }

@@ -22,6 +22,15 @@ constexpr double kSqrt2 = 1.41421356237;
 constexpr double kPi = 3.14159265359;
 constexpr double kGF = 1.16637E-11 * kMeV2;
 
+// Angle bins A and azimuth bins P of a configuration: SA has one trajectory
+// whatever Abins says (src/Phy_SA.cpp:150-184, beam_len = 2 Flvs), MA one
+// azimuth bin, MAA Pbins.  Beams = A P 4.
+inline void beam_dims(const xf_config& c, int& A, int& P)
+{
+    A = c.geometry == XF_GEOM_SA ? 1 : c.abins;
+    P = c.geometry == XF_GEOM_MAA ? c.pbins : 1;
+}
+
 struct Tables {
     int ne = 0;
     double dE = 0;
