@@ -12,32 +12,42 @@ using namespace detail;
 constexpr float kSeriesTF = 1.0f;
 
 // Taylor coefficients of cos(x) - 1 = sum_{k>=1} c_k t^k and
-// sin(x)/x = sum_{k>=0} s_k t^k, t = x^2; degree 5 keeps the truncation below
-// 4e-9 relative for t <= 1.
+// sin(x)/x = sum_{k>=0} s_k t^k, t = x^2.  Degree 5 keeps the truncation below
+// 4e-9 relative for t <= 1 (beyond, sqrt/sincos).  Degree 2 is used when every
+// lane of a warp has t <= kSmallT: the dropped terms are then below t^2/360 =
+// 2.5e-8 relative for the values and t^2/120 = 7.5e-8 for the divided
+// differences, under FP32's rounding; the workloads' accepted steps have t
+// around 1e-5 to 1e-3.
+constexpr float kSmallT = 3e-3f;
 __constant__ float kC[6] = {0.f, -0.5f, 1.f / 24.f, -1.f / 720.f, 1.f / 40320.f, -1.f / 3628800.f};
 __constant__ float kS[6] = {1.f, -1.f / 6.f, 1.f / 120.f, -1.f / 5040.f, 1.f / 362880.f, -1.f / 39916800.f};
+template <int DEG>
 __device__ __forceinline__ float horner(const float* c, float t)
 {
-    float p = c[5];
-    p = fmaf(p, t, c[4]);
-    p = fmaf(p, t, c[3]);
-    p = fmaf(p, t, c[2]);
-    p = fmaf(p, t, c[1]);
-    return fmaf(p, t, c[0]);
+    float p = c[DEG];
+#pragma unroll
+    for (int k = DEG - 1; k >= 0; --k) p = fmaf(p, t, c[k]);
+    return p;
 }
 
-// p(tB) and the divided difference p[tA, tB] = (p(tA) - p(tB)) / (tA - tB).
+// p(tB) and the divided difference p[tA, tB] = (p(tA) - p(tB)) / (tA - tB)
+// of the degree-DEG truncation.
+template <int DEG>
 __device__ __forceinline__ void divdiff(const float* c, float tA, float tB, float& pB, float& dd)
 {
-    float P = c[5], D = 0.f;
+    float P = c[DEG], D = 0.f;
 #pragma unroll
-    for (int k = 4; k >= 0; --k) {
+    for (int k = DEG - 1; k >= 0; --k) {
         D = fmaf(D, tA, P);
         P = fmaf(P, tB, c[k]);
     }
     pB = P;
     dd = D;
 }
+
+// Series degree for a warp whose largest t is tmax: 2 when every lane is
+// below kSmallT, else 5 (warp-uniform, so the branch does not diverge).
+__device__ __forceinline__ bool warp_small_t(float tmax) { return __all_sync(0xffffffffu, tmax <= kSmallT); }
 
 struct H3f {
     float h00, h01r, h01i;
@@ -97,13 +107,14 @@ struct KC {
     float cm1, S;
 };
 
+template <int DEG>
 __device__ __forceinline__ KC kcoef(const H3f& h, float l)
 {
     const float t = norm2(h) * (l * l);
     KC k;
-    if (t <= kSeriesTF) {
-        k.cm1 = horner(kC, t);
-        k.S = l * horner(kS, t);
+    if (DEG < 5 || t <= kSeriesTF) {
+        k.cm1 = horner<DEG>(kC, t);
+        k.S = l * horner<DEG>(kS, t);
     } else {
         const float x = sqrtf(t);
         float s, c;
@@ -119,51 +130,57 @@ __device__ __forceinline__ F4 k_apply(const KC& k, const H3f& h, const F4& x)
     return combine(k.cm1, x, scale(k.S, sig_apply(h, x)));
 }
 
-// [K(hA, l) - K(hB, l)] x given the accurate difference dh = hA - hB.
-__device__ __forceinline__ F4 diff_h(const H3f& hA, const H3f& hB, const H3f& dh, float l, const F4& x)
+__device__ __forceinline__ F4 sub(const F4& a, const F4& b)
+{
+    F4 c;
+    c.ar = a.ar - b.ar;
+    c.ai = a.ai - b.ai;
+    c.br = a.br - b.br;
+    c.bi = a.bi - b.bi;
+    return c;
+}
+
+// [K(hA, l) - K(hB, l)] x given the accurate difference dh = hA - hB and the
+// products sd = sigma(dh) x and sb = sigma(hB) x (sigma is linear in h, so
+// callers form sb from a product they already hold).
+template <int DEG>
+__device__ __forceinline__ F4 diff_h(const H3f& hA, const H3f& hB, const H3f& dh, float l, const F4& x, const F4& sd,
+                                     const F4& sb)
 {
     const float l2 = l * l;
     const float tA = norm2(hA) * l2, tB = norm2(hB) * l2;
-    if (tA > kSeriesTF || tB > kSeriesTF) {
-        const F4 a = k_apply(kcoef(hA, l), hA, x), b = k_apply(kcoef(hB, l), hB, x);
-        F4 r;
-        r.ar = a.ar - b.ar;
-        r.ai = a.ai - b.ai;
-        r.br = a.br - b.br;
-        r.bi = a.bi - b.bi;
-        return r;
+    if (DEG == 5 && (tA > kSeriesTF || tB > kSeriesTF)) {
+        const KC ka = kcoef<DEG>(hA, l), kb = kcoef<DEG>(hB, l);
+        return sub(combine(ka.cm1, x, scale(ka.S, add(sd, sb))), combine(kb.cm1, x, scale(kb.S, sb)));
     }
     const float dt = l2 * (dh.h00 * (hA.h00 + hB.h00) + dh.h01r * (hA.h01r + hB.h01r) + dh.h01i * (hA.h01i + hB.h01i));
     float cB, dc, sB, ds;
-    divdiff(kC, tA, tB, cB, dc);
-    divdiff(kS, tA, tB, sB, ds);
+    divdiff<DEG>(kC, tA, tB, cB, dc);
+    divdiff<DEG>(kS, tA, tB, sB, ds);
     const float SA = l * fmaf(dt, ds, sB);
     const float dS = l * (dt * ds);
-    const F4 v = add(scale(SA, sig_apply(dh, x)), scale(dS, sig_apply(hB, x)));
+    const F4 v = add(scale(SA, sd), scale(dS, sb));
     return combine(dt * dc, x, v);
 }
 
-// [K(h, lA) - K(h, lB)] x given the accurate difference dl = lA - lB.
-__device__ __forceinline__ F4 diff_l(const H3f& h, float lA, float lB, float dl, const F4& x)
+// [K(h, lA) - K(h, lB)] x given the accurate difference dl = lA - lB and the
+// product sh = sigma(h) x.
+template <int DEG>
+__device__ __forceinline__ F4 diff_l(const H3f& h, float lA, float lB, float dl, const F4& x, const F4& sh)
 {
     const float n2 = norm2(h);
     const float tA = n2 * lA * lA, tB = n2 * lB * lB;
-    if (tA > kSeriesTF || tB > kSeriesTF) {
-        const F4 a = k_apply(kcoef(h, lA), h, x), b = k_apply(kcoef(h, lB), h, x);
-        F4 r;
-        r.ar = a.ar - b.ar;
-        r.ai = a.ai - b.ai;
-        r.br = a.br - b.br;
-        r.bi = a.bi - b.bi;
-        return r;
+    if (DEG == 5 && (tA > kSeriesTF || tB > kSeriesTF)) {
+        const KC ka = kcoef<DEG>(h, lA), kb = kcoef<DEG>(h, lB);
+        return sub(combine(ka.cm1, x, scale(ka.S, sh)), combine(kb.cm1, x, scale(kb.S, sh)));
     }
     const float dt = n2 * dl * (lA + lB);
     float cB, dc, sB, ds;
-    divdiff(kC, tA, tB, cB, dc);
-    divdiff(kS, tA, tB, sB, ds);
+    divdiff<DEG>(kC, tA, tB, cB, dc);
+    divdiff<DEG>(kS, tA, tB, sB, ds);
     const float sA = fmaf(dt, ds, sB);
     const float dS = fmaf(dl, sA, lB * (dt * ds));
-    return combine(dt * dc, x, scale(dS, sig_apply(h, x)));
+    return combine(dt * dc, x, scale(dS, sh));
 }
 
 // Kahan-compensated FP32 accumulation (per thread, over its energies).
@@ -313,14 +330,19 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         for (int e = lane; e < epad; e += 32) {
             const H3f h = bin_hf(g0, d.hvf[e], d.hvf[epad + e]);
             const F4 x = load_f(in, epad, e);
-            const KC k0 = kcoef(h, l0);
-            KC k1;
+            const float lm = GEOM == 0 ? l0 : fmaxf(l0, l1);
+            KC k0, k1;
+            if (warp_small_t(norm2(h) * (lm * lm))) {
+                k0 = kcoef<2>(h, l0);
+                if (GEOM == 1) k1 = kcoef<2>(h, l1);
+            } else {
+                k0 = kcoef<5>(h, l0);
+                if (GEOM == 1) k1 = kcoef<5>(h, l1);
+            }
             if (GEOM == 0) {
                 // MA: dl1 = 2 dl0, so C1 - 1 = 2 (C0 - 1)(C0 + 1) and S1 = 2 C0 S0
                 k1.cm1 = 2.f * k0.cm1 * (k0.cm1 + 2.f);
                 k1.S = 2.f * (1.f + k0.cm1) * k0.S;
-            } else {
-                k1 = kcoef(h, l1);
             }
             const F4 u = sig_apply(h, x);
             const F4 d1 = combine(k1.cm1, x, scale(k1.S, u));
@@ -386,7 +408,8 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         for (int e = lane; e < epad; e += 32) {
             const H3f h = bin_hf(g3, d.hvf[e], d.hvf[epad + e]);
             const F4 x = load_f(in, epad, e);
-            acc_drho(x, k_apply(kcoef(h, l1), h, x), fvp[e], s0, s2, s3);
+            const KC k = warp_small_t(norm2(h) * (l1 * l1)) ? kcoef<2>(h, l1) : kcoef<5>(h, l1);
+            acc_drho(x, k_apply(k, h, x), fvp[e], s0, s2, s3);
         }
         double v[4] = {.5 * s0.value(), s2.value(), s3.value(), 0.};
         warp_reduce_scatter<4>(v, lane);
@@ -402,6 +425,37 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
 }
 
 // ------------------------------------------------------------------ phase C
+
+// One bin of phase C: the candidate increment inc = (d3' + d4m)/2 with
+// d3 = K(h0,l0) psi0, d3' = d3 + K(h4,l2)(psi0 + d3), d4m = K(h3,l1) psi0, and
+// t2 = 2 delta = psi4 - psi1 in difference form (see the file header).  The
+// sigma products of h1 and of h0 on psi3 follow from those of h3 and h4 by
+// linearity (sigma(h1) x = sigma(h3) x - sigma(h3 - h1) x).
+template <int DEG, int GEOM>
+__device__ __forceinline__ void c_bin(const H3f& h0, const H3f& h1, const H3f& h3, const H3f& h4, const H3f& d31,
+                                      const H3f& d40, float l0, float l1, float l2, float dl20, float dl01, const F4& x,
+                                      F4& inc, F4& t2)
+{
+    const KC k0 = kcoef<DEG>(h0, l0), k4 = kcoef<DEG>(h4, l2), k3 = kcoef<DEG>(h3, l1);
+    const F4 u0 = sig_apply(h0, x);
+    const F4 d3 = combine(k0.cm1, x, scale(k0.S, u0));
+    const F4 x3 = add(x, d3);
+    const F4 u4 = sig_apply(h4, x3);
+    const F4 d3p = add(d3, combine(k4.cm1, x3, scale(k4.S, u4)));
+    const F4 u3 = sig_apply(h3, x);
+    const F4 d4m = combine(k3.cm1, x, scale(k3.S, u3));
+    inc.ar = .5f * (d3p.ar + d4m.ar);
+    inc.ai = .5f * (d3p.ai + d4m.ai);
+    inc.br = .5f * (d3p.br + d4m.br);
+    inc.bi = .5f * (d3p.bi + d4m.bi);
+    const F4 sd31 = sig_apply(d31, x);
+    const F4 sd40 = sig_apply(d40, x3);
+    const F4 s0x3 = sub(u4, sd40);  // sigma(h0) psi3
+    t2 = diff_h<DEG>(h3, h1, d31, l1, x, sd31, sub(u3, sd31));
+    t2 = add(t2, diff_h<DEG>(h4, h0, d40, l2, x3, sd40, s0x3));
+    t2 = add(t2, diff_l<DEG>(h0, l2, l0, dl20, x3, s0x3));
+    if (GEOM == 1) t2 = add(t2, diff_l<DEG>(h0, 2.f * l0, l1, dl01, x, u0));
+}
 
 // Candidate psi4 = psi0 + (d3' + d4m)/2 with d3 = K(h0,l0) psi0,
 // d3' = d3 + K(h4,l2)(psi0 + d3), d4m = K(h3,l1) psi0; the error estimate in
@@ -460,16 +514,13 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             const H3f h0 = bin_hf(g0, hv0, hv1), h1 = bin_hf(g1, hv0, hv1);
             const H3f h3 = bin_hf(g3, hv0, hv1), h4 = bin_hf(g4, hv0, hv1);
             const F4 x = load_f(hi0 + base, epad, e);
-            const KC k0 = kcoef(h0, l0), k4 = kcoef(h4, l2), k3 = kcoef(h3, l1);
-            const F4 d3 = k_apply(k0, h0, x);
-            const F4 x3 = add(x, d3);
-            const F4 d3p = add(d3, k_apply(k4, h4, x3));
-            const F4 d4m = k_apply(k3, h3, x);
-            F4 inc;
-            inc.ar = .5f * (d3p.ar + d4m.ar);
-            inc.ai = .5f * (d3p.ai + d4m.ai);
-            inc.br = .5f * (d3p.br + d4m.br);
-            inc.bi = .5f * (d3p.bi + d4m.bi);
+            float lm = fmaxf(l0, l2);
+            if (GEOM == 1) lm = fmaxf(lm, fmaxf(2.f * l0, l1));
+            const float tmax = fmaxf(norm2(h0) * (lm * lm),
+                                     fmaxf(norm2(h4) * (l2 * l2), fmaxf(norm2(h3), norm2(h1)) * (l1 * l1)));
+            F4 inc, t2;
+            if (warp_small_t(tmax)) c_bin<2, GEOM>(h0, h1, h3, h4, d31, d40, l0, l1, l2, dl20, dl01, x, inc, t2);
+            else c_bin<5, GEOM>(h0, h1, h3, h4, d31, d40, l0, l1, l2, dl20, dl01, x, inc, t2);
             // candidate as a compensated pair
             const F4 xl = load_f(lo0 + base, epad, e);
             F4 ch, cl;
@@ -479,11 +530,6 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             ff_add(x.bi, xl.bi, inc.bi, ch.bi, cl.bi);
             store_f(hi4 + base, epad, e, ch);
             store_f(lo4 + base, epad, e, cl);
-            // 2 delta = psi4 - psi1 in difference form (see the file header)
-            F4 t2 = diff_h(h3, h1, d31, l1, x);
-            t2 = add(t2, diff_h(h4, h0, d40, l2, x3));
-            t2 = add(t2, diff_l(h0, l2, l0, dl20, x3));
-            if (GEOM == 1) t2 = add(t2, diff_l(h0, 2.f * l0, l1, dl01, x));
             const float f = fvp[e];
             err = fmaf(.25f * ((t2.ar * t2.ar + t2.ai * t2.ai) + (t2.br * t2.br + t2.bi * t2.bi)), f, err);
             acc_drho(x, inc, f, s0, s2, s3);
