@@ -97,6 +97,15 @@ __device__ __forceinline__ BeamH beam_offsets(const Dev& d, const double* J, int
 // 2: h01i part H3), with the same operations, for lane-parallel per-beam
 // set-up: a warp evaluates one scalar per lane and broadcasts them, instead of
 // every lane evaluating every scalar on the (slow) FP64 pipe.
+__device__ __forceinline__ BeamH shfl_beamh(double v, int first)
+{
+    BeamH h;
+    h.h00b = __shfl_sync(kFull, v, first);
+    h.h01rb = __shfl_sync(kFull, v, first + 1);
+    h.h01i = __shfl_sync(kFull, v, first + 2);
+    return h;
+}
+
 template <int GEOM>
 __device__ __forceinline__ double beam_offset_k(const Dev& d, const double* J, int pt, double hm, const BeamIdx& bi,
                                                 int k)

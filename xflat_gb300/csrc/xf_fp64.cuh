@@ -146,8 +146,12 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     const int myv = lane >> 2;  // value slot owned after an 8-way reduce-scatter
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
-        const BeamH h = beam_offsets<GEOM>(d, ctl->J0, 0, hm, bi);
-        const double dl1 = geo(d, 3, 1, bi.ang), dl0 = geo(d, 3, 0, bi.ang);
+        // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
+        double sv = 0.;
+        if (lane < 3) sv = beam_offset_k<GEOM>(d, ctl->J0, 0, hm, bi, lane);
+        else if (lane < 5) sv = geo(d, 3, lane - 3, bi.ang);
+        const BeamH h = shfl_beamh(sv, 0);
+        const double dl0 = __shfl_sync(kFull, sv, 3), dl1 = __shfl_sync(kFull, sv, 4);
         const double* in = psi0 + (size_t)b * 4 * epad;
         double* o1 = d.psi1 + (size_t)b * 4 * epad;
         double* o3 = d.psi3 + (size_t)b * 4 * epad;
@@ -219,9 +223,13 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
-        const BeamH g1 = beam_offsets<GEOM>(d, ctl->JA1, 2, hm_rdr, bi);
-        const BeamH g3 = beam_offsets<GEOM>(d, ctl->JA3, 1, hm_rdr2, bi);
-        const double dl1 = geo(d, 3, 1, bi.ang);
+        // lane-parallel set-up: lanes 0-2 the offsets of H1, 3-5 those of H3, lane 6 dl1
+        double sv = 0.;
+        if (lane < 3) sv = beam_offset_k<GEOM>(d, ctl->JA1, 2, hm_rdr, bi, lane);
+        else if (lane < 6) sv = beam_offset_k<GEOM>(d, ctl->JA3, 1, hm_rdr2, bi, lane - 3);
+        else if (lane == 6) sv = geo(d, 3, 1, bi.ang);
+        const BeamH g1 = shfl_beamh(sv, 0), g3 = shfl_beamh(sv, 3);
+        const double dl1 = __shfl_sync(kFull, sv, 6);
         const double* in = psi0 + (size_t)b * 4 * epad;
         double* io1 = d.psi1 + (size_t)b * 4 * epad;
         double* o4 = psi4 + (size_t)b * 4 * epad;
@@ -288,8 +296,12 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     const int myv = lane >> 3;  // 0: error, 1..3: density components 0, 2, 3
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
-        const BeamH g = beam_offsets<GEOM>(d, ctl->JB4, 2, hm_rdr, bi);
-        const double dl2 = geo(d, 3, 2, bi.ang);
+        // lane-parallel set-up: lanes 0-2 the offsets of H4, lane 3 dl2
+        double sv = 0.;
+        if (lane < 3) sv = beam_offset_k<GEOM>(d, ctl->JB4, 2, hm_rdr, bi, lane);
+        else if (lane == 3) sv = geo(d, 3, 2, bi.ang);
+        const BeamH g = shfl_beamh(sv, 0);
+        const double dl2 = __shfl_sync(kFull, sv, 3);
         double* io3 = d.psi3 + (size_t)b * 4 * epad;
         double* io4 = psi4 + (size_t)b * 4 * epad;
         const double* p1b = d.psi1 + (size_t)b * 4 * epad;
