@@ -90,3 +90,45 @@ def test_command_line_driver(tmp_path):
     assert snap.exists()
     out2 = subprocess.run([exe, str(cfg), str(snap)], capture_output=True, text=True, timeout=120)
     assert out2.returncode == 0 and "Provided data file" in out2.stdout
+
+
+@pytest.mark.parametrize("precision,iters", [("fp64", 40), ("mixed", 30)])
+def test_async_records_equal_states_of_each_accepted_step(tmp_path, precision, iters):
+    """Every accepted step is dumped; the asynchronous copies and the writer
+    thread must deliver, in order, exactly the state and survival of each
+    step while the stepper runs ahead."""
+    text = _cfg(tmp_path, r_step1="1e-12", r_step2="1e-12", Abins=16, Ebins=40).replace(
+        "precision= fp64", "precision= " + precision)
+    a = xg.Simulation(xg.Config.from_text(text))
+    o = xg._abi.XfRunOpts()
+    a.lib.xf_run_opts_default(o)
+    o.max_iters = iters
+    o.write_files = 1
+    st = xg._abi.XfRunStats()
+    assert a.lib.xf_run(a.h, o, xg._abi.XF_STEP_CB(0), None, st) == 0
+    # the files are complete when xf_run returns (before xf_io_close)
+    with scipy_io.netcdf_file(str(tmp_path / "runSnapshot0_0_.nc"), "r", mmap=False) as f:
+        psi = f.variables["psi"][:].copy()
+        r = f.variables["r"][:].copy()
+    with scipy_io.netcdf_file(str(tmp_path / "runProbability0_0_.nc"), "r", mmap=False) as f:
+        prob = np.stack([f.variables["prtcl%d" % p][:].reshape(len(r), -1) for p in range(4)], axis=-1)
+    assert a.lib.xf_io_close(a.h) == 0
+    # the same run stepped by hand, reading the state after every accepted step
+    b = xg.Simulation(xg.Config.from_text(text))
+    rr, dr = 20.0, 1e-5
+    states, surv, radii = [], [], []
+    eps0, ksi, maxdr = 1e-9, .94, .1
+    for _ in range(iters):
+        me = b.step(rr, dr)
+        if me < eps0:
+            rr += dr
+            b.accept()
+            states.append(b.get_state(0))
+            surv.append(b.survival())
+            radii.append(rr)
+        dr = min(dr * (ksi * np.sqrt(eps0 / me)), maxdr)  # src/Nmr.cpp:247 operation order
+    assert len(states) == st.accepted == len(r)
+    np.testing.assert_array_equal(r, radii)
+    for k in range(len(states)):
+        assert np.array_equal(psi[k].reshape(states[k].shape), states[k]), k
+        np.testing.assert_array_equal(prob[k].reshape(-1, 4), surv[k].reshape(-1, 4))

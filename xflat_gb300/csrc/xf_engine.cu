@@ -370,7 +370,10 @@ int xf_handle::run_host(const xf_run_opts& o, xf_step_cb cb, void* user, xf_run_
                 o.log[3 * acc + 2] = dr;
                 s.log_len = acc + 1;
             }
-            if (o.write_files && (rc = dump_files(it, r, dr))) return rc;
+            if (o.write_files && (rc = dump_files(it, r, dr))) {
+                flush_files();
+                return rc;
+            }
             acc++;
             if (cb && cb(user, it, r, dr)) {
                 it++;
@@ -386,6 +389,11 @@ int xf_handle::run_host(const xf_run_opts& o, xf_step_cb cb, void* user, xf_run_
     XF_CUDA(this, cudaEventSynchronize(ev[5]));
     float ms = 0.f;
     XF_CUDA(this, cudaEventElapsedTime(&ms, ev[4], ev[5]));
+    // the run's output records are complete when xf_run returns
+    if (o.write_files) {
+        const int frc = flush_files();
+        if (!rc) rc = frc;
+    }
     s.device_ms = ms;
     s.iterations = it;
     s.accepted = acc;
@@ -786,24 +794,15 @@ int xf_phase_times(const xf_handle* h, double* out, long* counts)
     return XF_OK;
 }
 
+// Per-beam survival of psi0 (src/IO_f.cpp:341-351), computed on the device.
 int xf_survival(xf_handle* h, double* out)
 {
     if (!h || !out) return XF_EINVAL;
-    std::vector<double> psi((size_t)h->nbeams * 4 * h->ne);
-    int rc = h->get_state(0, psi.data());
-    if (rc) return rc;
-    const int ne = h->ne, np = 4;
-    const int nbins = h->A * h->P;
-    for (int i = 0; i < nbins; ++i)
-        for (int p = 0; p < np; ++p) {
-            // src/IO_f.cpp:341-351: fv of beam (i*nbm_prtcls + p % nbm_flvs), i.e. particle p % 2
-            const double* fv = &h->tab.fv[(size_t)(p % 2) * ne];
-            const double* ar = &psi[((size_t)(i * np + p) * 4 + 0) * ne];
-            const double* ai = &psi[((size_t)(i * np + p) * 4 + 1) * ne];
-            double sum = 0.;
-            for (int e = 0; e < ne; ++e) sum += (ar[e] * ar[e] + ai[e] * ai[e]) * fv[e];
-            out[(size_t)i * np + p] = sum;
-        }
+    xf::launch_survival(h->dev, h->mixed != nullptr, h->d_Sscratch, h->st);
+    XF_CUDA(h, cudaGetLastError());
+    h->launches++;
+    XF_CUDA(h, cudaMemcpyAsync(out, h->d_Sscratch, (size_t)h->nbeams * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    XF_CUDA(h, cudaStreamSynchronize(h->st));
     return XF_OK;
 }
 

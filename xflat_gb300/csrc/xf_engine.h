@@ -86,4 +86,5 @@ struct xf_handle {
     int start_device_run(double r, double dr, long Ts);
     int get_graph(int k, bool timed, cudaGraphExec_t* out);
     int dump_files(long itr, double r, double dr);
+    int flush_files();  // waits until every queued output record is written
 };

@@ -3,16 +3,47 @@
 // Files, dimension and variable names, attribute names and values, dump
 // triggers, file rotation and sync follow src/IO_f.cpp:90-424 so existing
 // post-processing reads them unchanged.
+//
+// Output is asynchronous.  A dump decides its triggers on the calling thread
+// (as the reference does), then enqueues on the compute stream a kernel that
+// stages psi0 (or the per-beam survival) into a device buffer, and on a copy
+// stream the device-to-host copy of that buffer into one of two pinned host
+// buffers.  A writer thread waits for each copy and appends the record.  The
+// stepper therefore continues while a record is copied and written; it only
+// waits when both host buffers of a kind are still being written (disk slower
+// than the dumps) or when a device staging buffer is reused before its copy
+// has finished.  File creation and rotation drain the writer first and stay
+// synchronous, so their errors are reported by the dump that triggers them;
+// an append error is reported by the next dump, xf_io_close or the end of
+// xf_run.
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "xf_engine.h"
+#include "xf_kernels.h"
 #include "xf_netcdf.h"
 #include "xf_physics.h"
 #include "xflat_gpu.h"
+
+namespace {
+
+enum { JOB_SNAP = 0, JOB_PROB = 1 };
+
+struct Job {
+    int kind;
+    int buf;
+    double r, dr;
+    bool sync;
+};
+
+}  // namespace
 
 struct xf_io {
     xf::nc::Writer snap, prob;
@@ -22,6 +53,29 @@ struct xf_io {
     long t1 = 0, t2 = 0;       // wall seconds of the last time-triggered dumps
     bool inited = false;
     int verbose = 0;
+
+    // asynchronous pipeline (allocated at the first dump)
+    bool pipe = false;
+    int nbeams = 0;
+    cudaStream_t cs = nullptr;                // copy stream
+    double* d_state = nullptr;                // staged psi0, padded layout, big-endian
+    double* d_surv = nullptr;                 // staged survival, [nbeams]
+    double* h_state[2] = {nullptr, nullptr};  // pinned, unpadded [beam][comp][ebin], big-endian
+    double* h_surv[2] = {nullptr, nullptr};
+    cudaEvent_t staged = nullptr;             // compute stream: staging kernel done
+    cudaEvent_t state_copied[2] = {nullptr, nullptr}, surv_copied[2] = {nullptr, nullptr};
+    cudaEvent_t state_d2h = nullptr, surv_d2h = nullptr;  // last copy out of each staging buffer
+    bool state_d2h_pending = false, surv_d2h_pending = false;
+    int next_state = 0, next_surv = 0;
+
+    std::thread writer;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Job> q;
+    bool busy_state[2] = {false, false}, busy_surv[2] = {false, false};
+    bool working = false, stop = false;
+    int werr = 0;
+    std::string werr_msg;
 };
 
 namespace {
@@ -75,15 +129,179 @@ void snapshot_schema(const xf_config& c, std::vector<xf::nc::Dim>& dims, std::ve
     vars = {r, dr, psi};
 }
 
-// io_f::init (src/IO_f.cpp:90-194)
+// ---------------------------------------------------------------- writer thread
+
+// Appends queued records in order.  A record's host buffer is filled by a
+// copy on the copy stream; the writer waits for that copy's event first.
+void writer_main(xf_io* io, int device)
+{
+    cudaSetDevice(device);  // the handle's device, current in this thread too
+    std::vector<double> cols;
+    for (;;) {
+        Job j;
+        {
+            std::unique_lock<std::mutex> lk(io->mu);
+            io->cv.wait(lk, [io] { return io->stop || !io->q.empty(); });
+            if (io->q.empty()) return;  // stop requested and nothing left
+            j = io->q.front();
+            io->q.pop_front();
+            io->working = true;
+        }
+        bool ok = true;
+        std::string msg;
+        if (j.kind == JOB_SNAP) {
+            if (cudaEventSynchronize(io->state_copied[j.buf]) != cudaSuccess) {
+                ok = false;
+                msg = "snapshot copy failed";
+            } else if (!io->snap.append({&j.r, &j.dr, io->h_state[j.buf]}, {false, false, true})) {
+                ok = false;
+                msg = "snapshot write failed";
+            } else if (j.sync) {
+                io->snap.sync();
+            }
+        } else {
+            if (cudaEventSynchronize(io->surv_copied[j.buf]) != cudaSuccess) {
+                ok = false;
+                msg = "probability copy failed";
+            } else {
+                // per-particle columns prtcl0..3 over (theta, phi) (src/IO_f.cpp:341-384)
+                const int n = io->nbeams / 4;
+                cols.resize((size_t)4 * n);
+                const double* sv = io->h_surv[j.buf];
+                for (int i = 0; i < n; ++i)
+                    for (int p = 0; p < 4; ++p) cols[(size_t)p * n + i] = sv[(size_t)i * 4 + p];
+                if (!io->prob.append({&j.r, &cols[0], &cols[(size_t)n], &cols[2 * (size_t)n], &cols[3 * (size_t)n]})) {
+                    ok = false;
+                    msg = "probability write failed";
+                } else if (j.sync) {
+                    io->prob.sync();
+                }
+            }
+        }
+        {
+            std::lock_guard<std::mutex> lk(io->mu);
+            if (j.kind == JOB_SNAP) io->busy_state[j.buf] = false;
+            else io->busy_surv[j.buf] = false;
+            if (!ok && !io->werr) {
+                io->werr = XF_EIO;
+                io->werr_msg = msg;
+            }
+            io->working = false;
+        }
+        io->cv.notify_all();
+    }
+}
+
+// Waits until every queued record is written; returns the first writer error.
+int drain(xf_handle* h)
+{
+    xf_io& io = *h->io;
+    if (!io.pipe) return XF_OK;
+    std::unique_lock<std::mutex> lk(io.mu);
+    io.cv.wait(lk, [&io] { return io.q.empty() && !io.working; });
+    if (io.werr) return h->fail(io.werr, io.werr_msg);
+    return XF_OK;
+}
+
+int pipe_open(xf_handle* h)
+{
+    xf_io& io = *h->io;
+    if (io.pipe) return XF_OK;
+    io.nbeams = h->nbeams;
+    const size_t padded = (size_t)h->nbeams * 4 * h->epad, plain = (size_t)h->nbeams * 4 * h->ne;
+    auto ck = [h](cudaError_t e, const char* what) {
+        return e == cudaSuccess ? XF_OK : h->fail(XF_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    int rc;
+    if ((rc = ck(cudaStreamCreateWithFlags(&io.cs, cudaStreamNonBlocking), "copy stream"))) return rc;
+    if ((rc = ck(cudaMalloc((void**)&io.d_state, padded * sizeof(double)), "cudaMalloc"))) return rc;
+    if ((rc = ck(cudaMalloc((void**)&io.d_surv, (size_t)h->nbeams * sizeof(double)), "cudaMalloc"))) return rc;
+    for (int i = 0; i < 2; ++i) {
+        if ((rc = ck(cudaMallocHost((void**)&io.h_state[i], plain * sizeof(double)), "cudaMallocHost"))) return rc;
+        if ((rc = ck(cudaMallocHost((void**)&io.h_surv[i], (size_t)h->nbeams * sizeof(double)), "cudaMallocHost")))
+            return rc;
+        if ((rc = ck(cudaEventCreateWithFlags(&io.state_copied[i], cudaEventDisableTiming), "event"))) return rc;
+        if ((rc = ck(cudaEventCreateWithFlags(&io.surv_copied[i], cudaEventDisableTiming), "event"))) return rc;
+    }
+    if ((rc = ck(cudaEventCreateWithFlags(&io.staged, cudaEventDisableTiming), "event"))) return rc;
+    if ((rc = ck(cudaEventCreateWithFlags(&io.state_d2h, cudaEventDisableTiming), "event"))) return rc;
+    if ((rc = ck(cudaEventCreateWithFlags(&io.surv_d2h, cudaEventDisableTiming), "event"))) return rc;
+    io.stop = false;
+    io.writer = std::thread(writer_main, &io, h->device);
+    io.pipe = true;
+    return XF_OK;
+}
+
+void pipe_close(xf_io& io)
+{
+    if (io.writer.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(io.mu);
+            io.stop = true;
+        }
+        io.cv.notify_all();
+        io.writer.join();
+    }
+    if (io.cs) cudaStreamSynchronize(io.cs);
+    for (int i = 0; i < 2; ++i) {
+        if (io.h_state[i]) cudaFreeHost(io.h_state[i]);
+        if (io.h_surv[i]) cudaFreeHost(io.h_surv[i]);
+        if (io.state_copied[i]) cudaEventDestroy(io.state_copied[i]);
+        if (io.surv_copied[i]) cudaEventDestroy(io.surv_copied[i]);
+        io.h_state[i] = io.h_surv[i] = nullptr;
+        io.state_copied[i] = io.surv_copied[i] = nullptr;
+    }
+    if (io.d_state) cudaFree(io.d_state);
+    if (io.d_surv) cudaFree(io.d_surv);
+    if (io.staged) cudaEventDestroy(io.staged);
+    if (io.state_d2h) cudaEventDestroy(io.state_d2h);
+    if (io.surv_d2h) cudaEventDestroy(io.surv_d2h);
+    if (io.cs) cudaStreamDestroy(io.cs);
+    io.d_state = io.d_surv = nullptr;
+    io.staged = io.state_d2h = io.surv_d2h = nullptr;
+    io.cs = nullptr;
+    io.pipe = false;
+}
+
+// Claims host buffer `b` of a kind, waiting while the writer still uses it.
+int claim(xf_handle* h, bool* busy, int b)
+{
+    xf_io& io = *h->io;
+    std::unique_lock<std::mutex> lk(io.mu);
+    io.cv.wait(lk, [&] { return !busy[b] || io.werr; });
+    if (io.werr) return h->fail(io.werr, io.werr_msg);
+    busy[b] = true;
+    return XF_OK;
+}
+
+// Returns a claimed buffer when its copy could not be enqueued.
+void unclaim(xf_io& io, bool* busy, int b)
+{
+    std::lock_guard<std::mutex> lk(io.mu);
+    busy[b] = false;
+}
+
+void enqueue(xf_io& io, const Job& j)
+{
+    {
+        std::lock_guard<std::mutex> lk(io.mu);
+        io.q.push_back(j);
+    }
+    io.cv.notify_all();
+}
+
+// io_f::init (src/IO_f.cpp:90-194).  Drains the writer before touching files.
 int io_init(xf_handle* h, int ctr)
 {
     xf_io& io = *h->io;
     const xf_config& c = h->cfg;
+    int rc;
+    if ((rc = drain(h))) return rc;
+    io.snap.close();
+    io.prob.close();
     io.ctr = ctr;
     io.itr = 0;
     io.last_r0 = c.R0;
-    using xf::nc::Attr;
     using xf::nc::Dim;
     using xf::nc::Var;
     if (c.dump_mode & 1) {
@@ -108,53 +326,97 @@ int io_init(xf_handle* h, int ctr)
     return XF_OK;
 }
 
-void io_free(xf_io& io)
+// Stream-ordered staging of one record: `stage` fills the device buffer on the
+// compute stream after the step that produced the state; the copy stream then
+// moves it to the claimed host buffer.  The compute stream first waits for the
+// previous copy out of the same device buffer.
+template <typename Stage, typename Copy>
+int stage_and_copy(xf_handle* h, cudaEvent_t d2h, bool& d2h_pending, cudaEvent_t copied, Stage stage, Copy copy)
 {
-    io.snap.close();
-    io.prob.close();
-    io.inited = false;
+    xf_io& io = *h->io;
+    cudaError_t e = cudaSuccess;
+    if (d2h_pending) e = cudaStreamWaitEvent(h->st, d2h, 0);
+    if (e == cudaSuccess) {
+        stage();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(io.staged, h->st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(io.cs, io.staged, 0);
+    if (e == cudaSuccess) e = copy();
+    if (e == cudaSuccess) e = cudaEventRecord(copied, io.cs);
+    if (e == cudaSuccess) e = cudaEventRecord(d2h, io.cs);
+    if (e != cudaSuccess) return h->fail(XF_ECUDA, std::string("output staging: ") + cudaGetErrorString(e));
+    d2h_pending = true;
+    h->launches++;
+    return XF_OK;
 }
 
-// io_f::writeToFile for the snapshot (src/IO_f.cpp:266-328)
+// io_f::writeToFile for the snapshot (src/IO_f.cpp:266-328), asynchronous.
 int write_snapshot(xf_handle* h, double r, double dr)
 {
     xf_io& io = *h->io;
     const xf_config& c = h->cfg;
-    if ((int64_t)io.itr >= c.new_file_step) {
-        io.snap.close();
-        io.prob.close();
-        int rc = io_init(h, io.ctr + 1);
-        if (rc) return rc;
+    int rc;
+    if ((int64_t)io.itr >= c.new_file_step && (rc = io_init(h, io.ctr + 1))) return rc;
+    if ((rc = pipe_open(h))) return rc;
+    const int b = io.next_state;
+    if ((rc = claim(h, io.busy_state, b))) return rc;
+    rc = stage_and_copy(
+        h, io.state_d2h, io.state_d2h_pending, io.state_copied[b],
+        [&] { xf::launch_stage_state(h->dev, h->mixed != nullptr, 1, io.d_state, h->st); },
+        [&] {
+            return cudaMemcpy2DAsync(io.h_state[b], h->ne * sizeof(double), io.d_state, h->epad * sizeof(double),
+                                     h->ne * sizeof(double), (size_t)h->nbeams * 4, cudaMemcpyDeviceToHost, io.cs);
+        });
+    if (rc) {
+        unclaim(io, io.busy_state, b);
+        return rc;
     }
-    std::vector<double> psi((size_t)h->nbeams * 4 * h->ne);
-    int rc = h->get_state(0, psi.data());
-    if (rc) return rc;
-    if (!io.snap.append({&r, &dr, psi.data()})) return h->fail(XF_EIO, "snapshot write failed");
     io.itr++;
-    if (c.sync_step > 0 && io.itr % c.sync_step == 0) io.snap.sync();
+    enqueue(io, Job{JOB_SNAP, b, r, dr, c.sync_step > 0 && io.itr % c.sync_step == 0});
+    io.next_state ^= 1;
     return XF_OK;
 }
 
-// io_f::writeToFile for the probability file (src/IO_f.cpp:331-384)
+// io_f::writeToFile for the probability file (src/IO_f.cpp:331-384), asynchronous.
 int write_probability(xf_handle* h, double r)
 {
     xf_io& io = *h->io;
-    const int n = h->A * h->P;
-    std::vector<double> sv((size_t)n * 4);
-    int rc = xf_survival(h, sv.data());
-    if (rc) return rc;
-    std::vector<std::vector<double>> cols(4, std::vector<double>((size_t)n));
-    for (int i = 0; i < n; ++i)
-        for (int p = 0; p < 4; ++p) cols[p][i] = sv[(size_t)i * 4 + p];
-    if (!io.prob.append({&r, cols[0].data(), cols[1].data(), cols[2].data(), cols[3].data()}))
-        return h->fail(XF_EIO, "probability write failed");
-    if (h->cfg.sync_step > 0 && io.itr % h->cfg.sync_step == 0) io.prob.sync();
+    int rc;
+    if ((rc = pipe_open(h))) return rc;
+    const int b = io.next_surv;
+    if ((rc = claim(h, io.busy_surv, b))) return rc;
+    rc = stage_and_copy(
+        h, io.surv_d2h, io.surv_d2h_pending, io.surv_copied[b],
+        [&] { xf::launch_survival(h->dev, h->mixed != nullptr, io.d_surv, h->st); },
+        [&] {
+            return cudaMemcpyAsync(io.h_surv[b], io.d_surv, (size_t)h->nbeams * sizeof(double), cudaMemcpyDeviceToHost,
+                                   io.cs);
+        });
+    if (rc) {
+        unclaim(io, io.busy_surv, b);
+        return rc;
+    }
+    const int64_t ss = h->cfg.sync_step;
+    enqueue(io, Job{JOB_PROB, b, r, 0., ss > 0 && io.itr % ss == 0});
+    io.next_surv ^= 1;
     return XF_OK;
 }
 
 }  // namespace
 
 int xf_handle::dump_files(long it, double r, double dr) { return xf_dump(this, it, r, dr); }
+
+// Drains the writer and flushes both files (records and the header's record
+// count), so another reader sees every record written so far.
+int xf_handle::flush_files()
+{
+    if (!io) return XF_OK;
+    const int rc = drain(this);
+    io->snap.sync();
+    io->prob.sync();
+    return rc;
+}
 
 extern "C" {
 
@@ -167,6 +429,10 @@ int xf_dump(xf_handle* h, long it, double r, double dr)
     const xf_config& c = h->cfg;
     int rc;
     if (!io.inited && (rc = io_init(h, 0))) return rc;
+    {
+        std::lock_guard<std::mutex> lk(io.mu);
+        if (io.werr) return h->fail(io.werr, io.werr_msg);
+    }
     const long now = wall_s();
     if (!c.dump_mode) {
         if (r - io.last_r0 > 1.0) {
@@ -242,12 +508,16 @@ int xf_snapshot_read(const char* path, long rec, double* r, double* dr, double* 
 int xf_io_close(xf_handle* h)
 {
     if (!h) return XF_EINVAL;
+    int rc = XF_OK;
     if (h->io) {
-        io_free(*h->io);
+        rc = drain(h);
+        pipe_close(*h->io);
+        h->io->snap.close();
+        h->io->prob.close();
         delete h->io;
         h->io = nullptr;
     }
-    return XF_OK;
+    return rc;
 }
 
 int xf_io_verbose(xf_handle* h, int on)

@@ -128,6 +128,58 @@ __global__ void k_hvv_eval(Dev d, const double* __restrict__ J, int pt, double* 
     hvv[4 * i + 3] = H[2];
 }
 
+// The 8 bytes of v in reverse order: the halves swapped, each byte-reversed.
+__device__ __forceinline__ double byte_reversed(double v)
+{
+    const unsigned lo = (unsigned)__double2loint(v), hi = (unsigned)__double2hiint(v);
+    return __hiloint2double((int)__byte_perm(lo, 0, 0x0123), (int)__byte_perm(hi, 0, 0x0123));
+}
+
+// Reads psi0 through the control block, so the copy follows the role swaps of
+// accepted steps without a host round trip.
+__global__ void k_stage_state(Dev d, int mixed, int big_endian, double* __restrict__ dst)
+{
+    const Ctl* ctl = d.ctl;
+    const size_t n = (size_t)d.nbeams * 4 * d.epad;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const float* __restrict__ hi = ctl->m0hi;
+    const float* __restrict__ lo = ctl->m0lo;
+    const double* __restrict__ src = ctl->psi0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double v = mixed ? (double)hi[i] + (double)lo[i] : src[i];
+        dst[i] = big_endian ? byte_reversed(v) : v;
+    }
+}
+
+// One warp per beam; src/IO_f.cpp:346 weights beam i*4 + p with the spectrum
+// of particle p % 2 (an operator-precedence quirk kept for file parity).
+__global__ void k_survival(Dev d, int mixed, double* __restrict__ out)
+{
+    const Ctl* ctl = d.ctl;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int epad = d.epad;
+    for (int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < d.nbeams; b += nw) {
+        const double* fv = d.fv + (size_t)((b & 3) % 2) * epad;
+        const size_t base = (size_t)b * 4 * epad;
+        double s = 0.;
+        for (int e = lane; e < epad; e += 32) {
+            double ar, ai;
+            if (mixed) {
+                ar = (double)ctl->m0hi[base + e] + (double)ctl->m0lo[base + e];
+                ai = (double)ctl->m0hi[base + epad + e] + (double)ctl->m0lo[base + epad + e];
+            } else {
+                ar = ctl->psi0[base + e];
+                ai = ctl->psi0[base + epad + e];
+            }
+            s = fma(ar * ar + ai * ai, fv[e], s);
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
+        if (lane == 0) out[b] = s;
+    }
+}
+
 }  // namespace
 
 int max_phase_blocks(int nbeams, int threads)
@@ -179,6 +231,16 @@ void launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
 }
 
 void launch_accept(const Dev& d, cudaStream_t st) { k_accept<<<1, 1, 0, st>>>(d); }
+
+void launch_stage_state(const Dev& d, int mixed, int big_endian, double* dst, cudaStream_t st)
+{
+    k_stage_state<<<152 * 4, 256, 0, st>>>(d, mixed, big_endian, dst);
+}
+
+void launch_survival(const Dev& d, int mixed, double* out, cudaStream_t st)
+{
+    k_survival<<<max_phase_blocks(d.nbeams, 256), 256, 0, st>>>(d, mixed, out);
+}
 
 void launch_hvv_eval(const Dev& d, const double* J, int pt, double* hvv, cudaStream_t st)
 {

@@ -22,5 +22,13 @@ void launch_moments(const Dev& d, const double* S, int pt, double* Jout, cudaStr
 void launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st);
 void launch_accept(const Dev& d, cudaStream_t st);
 void launch_hvv_eval(const Dev& d, const double* J, int pt, double* hvv, cudaStream_t st);
+// FP64 copy of the accepted state psi0 (the mixed path's compensated pair
+// summed) in the padded [beam][comp][epad] layout, for output; with
+// big_endian set each double is stored byte-reversed (the NetCDF file
+// encoding on a little-endian host).
+void launch_stage_state(const Dev& d, int mixed, int big_endian, double* dst, cudaStream_t st);
+// Per-beam survival sum_e fv (ar^2 + ai^2) of psi0 (the Probability file's
+// quantity, src/IO_f.cpp:341-351), out[nbeams].
+void launch_survival(const Dev& d, int mixed, double* out, cudaStream_t st);
 
 }  // namespace xf

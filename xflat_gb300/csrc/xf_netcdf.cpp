@@ -173,19 +173,32 @@ bool Writer::create(const std::string& path, const std::vector<Dim>& dims, const
 
 bool Writer::append(const std::vector<const double*>& data)
 {
+    return append(std::vector<const void*>(data.begin(), data.end()), std::vector<bool>(data.size(), false));
+}
+
+bool Writer::append(const std::vector<const void*>& data, const std::vector<bool>& be)
+{
     if (!f_) return false;
     std::vector<uint8_t> buf;
     size_t k = 0;
     for (const auto& v : vars_) {
         if (!v.record) continue;
+        if (k >= data.size()) return false;
         uint64_t n = 1;
         for (size_t i = 1; i < v.dims.size(); ++i) n *= dims_[v.dims[i]].len;
-        buf.assign((size_t)v.vsize, 0);
-        for (uint64_t i = 0; i < n; ++i) put_double_be(&buf[8 * i], data[k][i]);
         const uint64_t off = v.begin + numrecs_ * recsize_;
         if (std::fseek(f_, (long)off, SEEK_SET) != 0) return false;
-        const size_t len = (recsize_ < v.vsize) ? (size_t)recsize_ : buf.size();
-        if (std::fwrite(buf.data(), 1, len, f_) != len) return false;
+        // a lone record variable is not padded to 4 bytes in the record (the format's special case)
+        const size_t len = (recsize_ < v.vsize) ? (size_t)recsize_ : (size_t)v.vsize;
+        if (k < be.size() && be[k]) {
+            // doubles are 8 bytes, so the slab has no padding: n * 8 == vsize
+            if (std::fwrite(data[k], 1, len, f_) != len) return false;
+        } else {
+            buf.assign((size_t)v.vsize, 0);
+            const double* d = static_cast<const double*>(data[k]);
+            for (uint64_t i = 0; i < n; ++i) put_double_be(&buf[8 * i], d[i]);
+            if (std::fwrite(buf.data(), 1, len, f_) != len) return false;
+        }
         ++k;
     }
     ++numrecs_;

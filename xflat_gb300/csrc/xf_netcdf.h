@@ -40,6 +40,9 @@ public:
     bool create(const std::string& path, const std::vector<Dim>& dims, const std::vector<Var>& vars, int version = 2);
     // Appends one record: data[i] holds the slab of the i-th record variable.
     bool append(const std::vector<const double*>& data);
+    // The same with some slabs already in the file's big-endian encoding
+    // (be[i] set): those are written as given, without conversion.
+    bool append(const std::vector<const void*>& data, const std::vector<bool>& be);
     bool sync();
     void close();
     uint64_t records() const { return numrecs_; }
