@@ -217,15 +217,20 @@ int xf_probe_fp64_peak(double ms, double* tflops);
 /* ---------------------------------------------------------------- files */
 /* The reference's NetCDF IO module (src/IO_f.cpp), written without libnetcdf
  * in the classic format (64-bit offsets): file names <prefix>Snapshot<n>_0_.nc
- * (dims r[unlimited], theta, [phi], prtcl, comp, ebin; variables r, dr, psi)
- * and <prefix>Probability<n>_0_.nc (dims r, theta, phi; variables r,
- * prtcl0..prtcl3).
+ * (dims r[unlimited], theta (not for SA), [phi], prtcl, comp, ebin; variables
+ * r, dr, psi) and <prefix>Probability<n>_0_.nc (dims r, theta, phi; variables
+ * r, prtcl0..prtcl3).
  * xf_dump: fio::dumpToFile (src/IO_f.cpp:387-424) with the same radius, time
  *   and iteration triggers, file rotation every new_file_step records and
- *   sync every sync_step; files are created on the first call.
+ *   sync every sync_step; files are created on the first call.  The record is
+ *   the state at the call, stream-ordered; it is staged on the device, copied
+ *   to pinned host memory on a copy stream and appended by a writer thread,
+ *   so the call returns without waiting for the copy or the write.  A failed
+ *   append is reported by the next xf_dump, xf_io_close or the end of xf_run;
+ *   xf_run (write_files) returns with every record written and flushed.
  * xf_resume: fio::fillInitData (src/IO_f.cpp:197-250): psi0 and the last r
  *   and dr from the last record of a Snapshot file.
- * xf_io_close: fio::freemem (src/IO_f.cpp:252-263).
+ * xf_io_close: fio::freemem (src/IO_f.cpp:252-263); waits for pending records.
  * xf_io_verbose: print the radius on dumps, as the reference does (default off). */
 int xf_dump(xf_handle* h, long itr, double r, double dr);
 int xf_resume(xf_handle* h, const char* path, double* r, double* dr);
