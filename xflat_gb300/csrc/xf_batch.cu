@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "xf_common.cuh"
+#include "xf_launch.cuh"
 #include "xf_engine.h"
 #include "xf_fp64.cuh"
 #include "xf_mixed.cuh"
@@ -57,6 +58,7 @@ __device__ __forceinline__ RedTarget tile_target(const Dev& d, const Tile& t, in
 
 __global__ void k_batch_geometry(const Dev* __restrict__ devs, const int2* __restrict__ angles, int n)
 {
+    xf::pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int2 a = angles[i];
@@ -72,6 +74,7 @@ template <int PREC, int PH>
 __global__ void __launch_bounds__(256, batch_min_blocks<PREC, PH>()) k_batch_phase(const Dev* __restrict__ devs,
                                                                                      const Tile* __restrict__ tiles)
 {
+    xf::pdl_enter();
     const Tile t = tiles[blockIdx.x];
     const Dev& d = devs[t.inst];
     const RedTarget rt = tile_target(d, t, PH);
@@ -90,12 +93,14 @@ __global__ void __launch_bounds__(256, batch_min_blocks<PREC, PH>()) k_batch_pha
 // and the refreshed moments of psi0 (thread tiles of 256 beams).
 __global__ void __launch_bounds__(256) k_batch_renorm(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
 {
+    xf::pdl_enter();
     const Tile t = tiles[blockIdx.x];
     xf::mixed::esum_body(devs[t.inst], t.first, devs[t.inst].nbeams, 1, 1);
 }
 
 __global__ void __launch_bounds__(256) k_batch_moments(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
 {
+    xf::pdl_enter();
     const Tile t = tiles[blockIdx.x];
     const Dev& d = devs[t.inst];
     moments_body<0>(d, t.first, d.nbeams, tile_target(d, t, xf::PH_MOM), nullptr, 0, &d.ctl->J0[0], 1);
@@ -224,17 +229,19 @@ int build_lists(xf_batch* b, int warps)
 void launch_iteration(xf_batch* b)
 {
     const int threads = 32 * b->warps;
-    k_batch_geometry<<<(b->nang + 127) / 128, 128, 0, b->st>>>(b->d_devs, b->d_angles, b->nang);
+    const Dev* dv = b->d_devs;
+    const Tile* wt = b->d_wtiles;
+    xf::launch_pdl(k_batch_geometry, (b->nang + 127) / 128, 128, b->st, dv, (const int2*)b->d_angles, b->nang);
     if (b->prec == XF_PREC_MIXED) {
-        k_batch_renorm<<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
-        k_batch_moments<<<b->ntt, 256, 0, b->st>>>(b->d_devs, b->d_ttiles);
-        k_batch_phase<1, xf::PH_A><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
-        k_batch_phase<1, xf::PH_B><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
-        k_batch_phase<1, xf::PH_C><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        xf::launch_pdl(k_batch_renorm, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_moments, b->ntt, 256, b->st, dv, (const Tile*)b->d_ttiles);
+        xf::launch_pdl(k_batch_phase<1, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<1, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<1, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
     } else {
-        k_batch_phase<0, xf::PH_A><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
-        k_batch_phase<0, xf::PH_B><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
-        k_batch_phase<0, xf::PH_C><<<b->nwt, threads, 0, b->st>>>(b->d_devs, b->d_wtiles);
+        xf::launch_pdl(k_batch_phase<0, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<0, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<0, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
     }
 }
 

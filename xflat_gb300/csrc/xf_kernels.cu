@@ -27,6 +27,7 @@
 #include "xf_kernels.h"
 
 #include "xf_common.cuh"
+#include "xf_launch.cuh"
 #include "xf_fp64.cuh"
 
 #include <algorithm>
@@ -42,7 +43,11 @@ using namespace detail;
 // path segments (src/Nmr.cpp:153-173, src/Phy_MA.cpp:172-227,
 // src/Phy_MAA.cpp:194-241).  Under device control thread 0 also evaluates the
 // matter term at the three points (src/Matt.cpp:31-64).
-__global__ void k_geometry(Dev d) { geometry_body(d, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_geometry(Dev d)
+{
+    pdl_enter();
+    geometry_body(d, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ------------------------------------------------------------------ phases
 
@@ -51,18 +56,21 @@ __global__ void k_geometry(Dev d) { geometry_body(d, blockIdx.x * blockDim.x + t
 template <int GEOM>
 __global__ void __launch_bounds__(256) k_phaseA(Dev d)
 {
+    pdl_enter();
     fp64::phaseA_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_A));
 }
 
 template <int GEOM>
 __global__ void __launch_bounds__(256) k_phaseB(Dev d)
 {
+    pdl_enter();
     fp64::phaseB_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_B));
 }
 
 template <int GEOM>
 __global__ void __launch_bounds__(256) k_phaseC(Dev d)
 {
+    pdl_enter();
     fp64::phaseC_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_C));
 }
 
@@ -92,6 +100,7 @@ template <int GEOM>
 __global__ void __launch_bounds__(256) k_moments(Dev d, const double* __restrict__ Sarg, int pt, double* Jout,
                                                  int conditional)
 {
+    pdl_enter();
     moments_body<GEOM>(d, blockIdx.x * blockDim.x, gridDim.x * blockDim.x, grid_target(d, PH_MOM), Sarg, pt, Jout,
                        conditional);
 }
@@ -201,7 +210,7 @@ Shape default_shape(int nbeams, int epad)
 void launch_geometry(const Dev& d, cudaStream_t st)
 {
     const int t = 128;
-    k_geometry<<<(d.A + t - 1) / t, t, 0, st>>>(d);
+    launch_pdl(k_geometry, (d.A + t - 1) / t, t, st, d);
 }
 
 void launch_esum(const Dev& d, const double* psi, double* S, cudaStream_t st)
@@ -213,20 +222,20 @@ void launch_moments(const Dev& d, const double* S, int pt, double* Jout, cudaStr
 {
     const int t = 256;
     const int blocks = std::max(1, std::min((d.nbeams + t - 1) / t, 152 * 4));
-    if (d.geom == 0) k_moments<0><<<blocks, t, 0, st>>>(d, S, pt, Jout, conditional);
-    else k_moments<1><<<blocks, t, 0, st>>>(d, S, pt, Jout, conditional);
+    if (d.geom == 0) launch_pdl(k_moments<0>, blocks, t, st, d, S, pt, Jout, conditional);
+    else launch_pdl(k_moments<1>, blocks, t, st, d, S, pt, Jout, conditional);
 }
 
 void launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
 {
     if (d.geom == 0) {
-        if (phase == PH_A) k_phaseA<0><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else if (phase == PH_B) k_phaseB<0><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else k_phaseC<0><<<sh.blocks, sh.threads, 0, st>>>(d);
+        if (phase == PH_A) launch_pdl(k_phaseA<0>, sh.blocks, sh.threads, st, d);
+        else if (phase == PH_B) launch_pdl(k_phaseB<0>, sh.blocks, sh.threads, st, d);
+        else launch_pdl(k_phaseC<0>, sh.blocks, sh.threads, st, d);
     } else {
-        if (phase == PH_A) k_phaseA<1><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else if (phase == PH_B) k_phaseB<1><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else k_phaseC<1><<<sh.blocks, sh.threads, 0, st>>>(d);
+        if (phase == PH_A) launch_pdl(k_phaseA<1>, sh.blocks, sh.threads, st, d);
+        else if (phase == PH_B) launch_pdl(k_phaseB<1>, sh.blocks, sh.threads, st, d);
+        else launch_pdl(k_phaseC<1>, sh.blocks, sh.threads, st, d);
     }
 }
 

@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "xf_common.cuh"
+#include "xf_launch.cuh"
 #include "xf_mixed.cuh"
 #include "xf_engine.h"
 #include "xf_kernels.h"
@@ -55,18 +56,21 @@ using mixed::KSum;
 template <int GEOM>
 __global__ void __launch_bounds__(256, 5) k_mixA(Dev d)
 {
+    pdl_enter();
     mixed::phaseA_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_A));
 }
 
 template <int GEOM>
 __global__ void __launch_bounds__(256, 6) k_mixB(Dev d)
 {
+    pdl_enter();
     mixed::phaseB_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_B));
 }
 
 template <int GEOM>
 __global__ void __launch_bounds__(256, 4) k_mixC(Dev d)
 {
+    pdl_enter();
     mixed::phaseC_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_C));
 }
 
@@ -79,6 +83,7 @@ __global__ void __launch_bounds__(256, 4) k_mixC(Dev d)
 // renormalisation (every renorm_every accepted steps under device control).
 __global__ void __launch_bounds__(256) k_mix_esum(Dev d, int renorm, int conditional)
 {
+    pdl_enter();
     mixed::esum_body(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), renorm, conditional);
 }
 
@@ -212,13 +217,13 @@ int mixed_get_state(xf_handle* h, Mixed* m, int which, double* psi)
 void mixed_launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
 {
     if (d.geom == 0) {
-        if (phase == PH_A) k_mixA<0><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else if (phase == PH_B) k_mixB<0><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else k_mixC<0><<<sh.blocks, sh.threads, 0, st>>>(d);
+        if (phase == PH_A) launch_pdl(k_mixA<0>, sh.blocks, sh.threads, st, d);
+        else if (phase == PH_B) launch_pdl(k_mixB<0>, sh.blocks, sh.threads, st, d);
+        else launch_pdl(k_mixC<0>, sh.blocks, sh.threads, st, d);
     } else {
-        if (phase == PH_A) k_mixA<1><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else if (phase == PH_B) k_mixB<1><<<sh.blocks, sh.threads, 0, st>>>(d);
-        else k_mixC<1><<<sh.blocks, sh.threads, 0, st>>>(d);
+        if (phase == PH_A) launch_pdl(k_mixA<1>, sh.blocks, sh.threads, st, d);
+        else if (phase == PH_B) launch_pdl(k_mixB<1>, sh.blocks, sh.threads, st, d);
+        else launch_pdl(k_mixC<1>, sh.blocks, sh.threads, st, d);
     }
 }
 
@@ -226,7 +231,12 @@ void mixed_launch_accept(const Dev& d, cudaStream_t st) { k_mix_accept<<<1, 1, 0
 
 void mixed_launch_renorm(const Dev& d, int conditional, cudaStream_t st)
 {
-    k_mix_esum<<<max_phase_blocks(d.nbeams, 256), 256, 0, st>>>(d, 1, conditional);
+    // The conditional form runs every iteration of a device-controlled graph
+    // and usually finds nothing to do: a grid of two blocks per SM keeps that
+    // empty launch cheap, and covers the beams grid-stride when it does work.
+    const int blocks = conditional ? std::min(max_phase_blocks(d.nbeams, 256), 2 * 152)
+                                   : max_phase_blocks(d.nbeams, 256);
+    launch_pdl(k_mix_esum, blocks, 256, st, d, 1, conditional);
 }
 
 }  // namespace xf
