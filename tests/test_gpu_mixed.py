@@ -115,3 +115,29 @@ def test_sa_free_running_window_vs_fp64():
     if oa["accepted"] == ob["accepted"]:
         d = np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0))))
         assert d <= 1e-5, d
+
+
+@pytest.mark.parametrize("geom", ["config0_ma.txt", "config3_maa.txt"])
+def test_renormalised_sums_match_oracle(geom):
+    """The renormalisation recomputes psi0's energy sums (the anchor of the
+    differential moments) in double-float arithmetic: the Hamiltonian built
+    from them agrees with the oracle's, computed in FP64 from the same state,
+    to 1e-12 of its scale."""
+    from helpers import TempConfig
+    from oracle.port import Port
+    text = derive(geom, Abins=12, Pbins=3, Ebins=40, R0=20, dr="1e-6")
+    b = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= mixed")))
+    assert b.lib.xf_set_option(b.h, b"renorm_every", 1.0) == 0
+    # host-driven: every accepted step is renormalised at once, so psi0's sums are the renormalised ones
+    out = b.evolutionLoop(max_iters=30)
+    assert out["accepted"] > 0
+    psi = b.get_state(0)
+    with TempConfig(text) as path:
+        port = Port(path)
+    port.set_state(psi)
+    r, dr = out["r_end"], out["dr_end"]
+    for pt in range(3):
+        h = b.calc_Hvv(0, pt, r, dr).reshape(-1)
+        port.probe(r, dr)
+        ref = port.calc_hvv(0, pt).reshape(-1)
+        assert np.max(np.abs(h - ref)) <= 1e-12 * np.max(np.abs(ref)), pt

@@ -60,6 +60,7 @@ struct Dev {
     const double* fv;     // [4][epad]
     const double* hvac;   // [2][epad]: h00 part, then h01 real part
     const float* fvf;     // FP32 copies for the mixed-precision kernels
+    const float* fvf_lo;  // fv - fvf rounded to FP32: (fvf, fvf_lo) is fv as a double-float
     const float* hvf;
     const double* cos2R;  // [A]
     const double* dcos2R; // [A]

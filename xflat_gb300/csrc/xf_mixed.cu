@@ -111,6 +111,7 @@ struct Mixed {
     float* hi[2] = {nullptr, nullptr};
     float* lo[2] = {nullptr, nullptr};
     float* fvf = nullptr;
+    float* fvf_lo = nullptr;
     float* hvf = nullptr;
     double* S[2] = {nullptr, nullptr};
 };
@@ -131,15 +132,21 @@ Mixed* mixed_create(xf_handle* h)
         ok = ok && cudaMalloc(&m->lo[i], n * sizeof(float)) == cudaSuccess && cudaMemset(m->lo[i], 0, n * sizeof(float)) == cudaSuccess;
         ok = ok && cudaMalloc(&m->S[i], 4 * (size_t)h->nbeams * sizeof(double)) == cudaSuccess;
     }
-    std::vector<float> fvf(4 * (size_t)h->epad, 0.f), hvf(2 * (size_t)h->epad, 0.f);
+    std::vector<float> fvf(4 * (size_t)h->epad, 0.f), fvf_lo(4 * (size_t)h->epad, 0.f), hvf(2 * (size_t)h->epad, 0.f);
     for (int p = 0; p < 4; ++p)
-        for (int e = 0; e < h->ne; ++e) fvf[(size_t)p * h->epad + e] = (float)h->tab.fv[(size_t)p * h->ne + e];
+        for (int e = 0; e < h->ne; ++e) {
+            const double f = h->tab.fv[(size_t)p * h->ne + e];
+            fvf[(size_t)p * h->epad + e] = (float)f;
+            fvf_lo[(size_t)p * h->epad + e] = (float)(f - (double)(float)f);
+        }
     for (int e = 0; e < h->ne; ++e) {
         hvf[e] = (float)h->tab.hvac[2 * (size_t)e];
         hvf[h->epad + e] = (float)h->tab.hvac[2 * (size_t)e + 1];
     }
     ok = ok && cudaMalloc(&m->fvf, fvf.size() * sizeof(float)) == cudaSuccess &&
          cudaMemcpy(m->fvf, fvf.data(), fvf.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMalloc(&m->fvf_lo, fvf_lo.size() * sizeof(float)) == cudaSuccess &&
+         cudaMemcpy(m->fvf_lo, fvf_lo.data(), fvf_lo.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMalloc(&m->hvf, hvf.size() * sizeof(float)) == cudaSuccess &&
          cudaMemcpy(m->hvf, hvf.data(), hvf.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     if (!ok) {
@@ -148,6 +155,7 @@ Mixed* mixed_create(xf_handle* h)
         return nullptr;
     }
     h->dev.fvf = m->fvf;
+    h->dev.fvf_lo = m->fvf_lo;
     h->dev.hvf = m->hvf;
     h->h_ctl->m0hi = m->hi[0];
     h->h_ctl->m0lo = m->lo[0];
@@ -172,6 +180,7 @@ void mixed_destroy(Mixed* m)
         if (m->S[i]) cudaFree(m->S[i]);
     }
     if (m->fvf) cudaFree(m->fvf);
+    if (m->fvf_lo) cudaFree(m->fvf_lo);
     if (m->hvf) cudaFree(m->hvf);
     delete m;
 }

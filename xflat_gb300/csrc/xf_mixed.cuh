@@ -570,10 +570,97 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     }
 }
 
-// Exact FP64 energy sums of psi0 from its compensated pairs (NBeam::calcESum,
+// ------------------------------------------------------------------ double-float
+
+// Error-free transformations on FP32 (the compensated pairs' arithmetic):
+// TwoSum (Knuth), Fast2Sum (Dekker, |a| >= |b|) and the FMA-based TwoProduct.
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ DF two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bp = s - a;
+    return DF{s, (a - (s - bp)) + (b - bp)};
+}
+
+__device__ __forceinline__ DF fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+
+__device__ __forceinline__ DF two_prod(float a, float b)
+{
+    const float p = a * b;
+    return DF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ DF df_add(const DF& a, const DF& b)
+{
+    const DF s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, s.l + (a.l + b.l));
+}
+
+__device__ __forceinline__ DF df_mul(const DF& a, const DF& b)
+{
+    const DF p = two_prod(a.h, b.h);
+    return fast_two_sum(p.h, fmaf(a.h, b.l, fmaf(a.l, b.h, p.l)));
+}
+
+// x0 x1 + y0 y1 for compensated pairs x = (x0 + xl0), ... (the lo*lo terms,
+// 2^-48 of the result, are dropped).
+__device__ __forceinline__ DF df_dot2(float x0, float xl0, float x1, float xl1, float y0, float yl0, float y1,
+                                      float yl1)
+{
+    const DF p = two_prod(x0, x1), q = two_prod(y0, y1);
+    const DF t = two_sum(p.h, q.h);
+    const float cross = fmaf(x0, xl1, fmaf(xl0, x1, fmaf(y0, yl1, yl0 * y1)));
+    return fast_two_sum(t.h, t.l + (p.l + q.l + cross));
+}
+
+// ------------------------------------------------------------------ esum / renormalisation
+
+// Energy sums of psi0 from its compensated pairs (NBeam::calcESum,
 // src/NBeam.cpp:812-840), optionally after the unitarity renormalisation of
-// every bin (|a|^2 + |b|^2 = 1 in FP64, written back as compensated pairs);
-// with `conditional` only when the step controller flagged a renormalisation.
+// every bin (|a|^2 + |b|^2 = 1, written back as compensated pairs); with
+// `conditional` only when the step controller flagged a renormalisation.
+//
+// Without renormalisation (a state handed in by the host) the sums are FP64.
+// The renormalisation, which runs every few accepted steps inside the
+// stepping loop, stays off the FP64 pipe: n - 1 of a bin is formed in
+// double-float arithmetic (the pairs carry 48 bits), the bin is scaled by
+// 1 + dn (-1/2 + 3 dn/8) = 1/sqrt(n) to rounding for |dn| < 1e-6 (next term
+// 5|dn|^3/16), and the density moments are accumulated in double-float per
+// thread (weights fv as double-float pairs) and in FP64 across threads.  A
+// bin whose norm has drifted further is renormalised in FP64.
+__device__ __forceinline__ void renorm_bin_fp64(float* ph, float* pl, int epad, int e, double fe, DF* acc)
+{
+    double a[4];
+    double n = 0.;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        a[k] = (double)ph[k * epad + e] + (double)pl[k * epad + e];
+        n = fma(a[k], a[k], n);
+    }
+    const double f = 1. / sqrt(n);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        a[k] *= f;
+        const float ah = (float)a[k];
+        ph[k * epad + e] = ah;
+        pl[k * epad + e] = (float)(a[k] - (double)ah);
+    }
+    const double r[3] = {((a[0] * a[0] + a[1] * a[1]) - (a[2] * a[2] + a[3] * a[3])) * fe,
+                         (a[0] * a[2] + a[1] * a[3]) * fe, (a[1] * a[2] - a[0] * a[3]) * fe};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float rh = (float)r[k];
+        acc[k] = df_add(acc[k], DF{rh, (float)(r[k] - (double)rh)});
+    }
+}
+
 __device__ inline void esum_body(const Dev& d, int first, int stride, int renorm, int conditional)
 {
     Ctl* ctl = d.ctl;
@@ -587,36 +674,64 @@ __device__ inline void esum_body(const Dev& d, int first, int stride, int renorm
     for (int b = gw; b < d.nbeams; b += tw) {
         float* ph = hi + (size_t)b * 4 * epad;
         float* pl = lo + (size_t)b * 4 * epad;
-        const double* fvp = d.fv + (b & 3) * epad;
         double v[4] = {0., 0., 0., 0.};
-        for (int e = lane; e < epad; e += 32) {
-            double a[4];
-            double n = 0.;
+        if (!renorm) {
+            const double* fvp = d.fv + (b & 3) * epad;
+            for (int e = lane; e < epad; e += 32) {
+                double a[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                a[k] = (double)ph[k * epad + e] + (double)pl[k * epad + e];
-                n = fma(a[k], a[k], n);
+                for (int k = 0; k < 4; ++k) a[k] = (double)ph[k * epad + e] + (double)pl[k * epad + e];
+                const double fe = fvp[e];
+                v[1] = fma((a[0] * a[0] + a[1] * a[1]) - (a[2] * a[2] + a[3] * a[3]), fe, v[1]);
+                v[2] = fma(a[0] * a[2] + a[1] * a[3], fe, v[2]);
+                v[3] = fma(a[1] * a[2] - a[0] * a[3], fe, v[3]);
             }
-            if (renorm && n > 0.) {
-                // 1/sqrt(n) for n = 1 + dn: the series 1 - dn/2 + 3 dn^2/8 is
-                // exact to rounding for |dn| < 1e-6 (next term 5|dn|^3/16 <
-                // 4e-19), which the compensated state keeps between
-                // renormalisations; two FMAs instead of a sqrt and a division
-                // on the FP64 pipe.
-                const double dn = n - 1.;
-                const double f = fabs(dn) < 1e-6 ? fma(dn, fma(dn, .375, -.5), 1.) : 1. / sqrt(n);
+        } else {
+            const float* fh = d.fvf + (b & 3) * epad;
+            const float* fl = d.fvf_lo + (b & 3) * epad;
+            DF acc[3] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
+            for (int e = lane; e < epad; e += 32) {
+                float h[4], l[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    a[k] *= f;
-                    const float ah = (float)a[k];
-                    ph[k * epad + e] = ah;
-                    pl[k * epad + e] = (float)(a[k] - (double)ah);
+                    h[k] = ph[k * epad + e];
+                    l[k] = pl[k * epad + e];
                 }
+                // n = sum (h + l)^2 as s + c: squares by TwoProduct, summed by TwoSum
+                const DF q0 = two_prod(h[0], h[0]), q1 = two_prod(h[1], h[1]);
+                const DF q2 = two_prod(h[2], h[2]), q3 = two_prod(h[3], h[3]);
+                const DF s01 = two_sum(q0.h, q1.h), s23 = two_sum(q2.h, q3.h);
+                const DF sn = two_sum(s01.h, s23.h);
+                if (sn.h == 0.f) continue;  // padding bin
+                const float cross = 2.f * fmaf(h[0], l[0], fmaf(h[1], l[1], fmaf(h[2], l[2], h[3] * l[3])));
+                const float c = sn.l + (s01.l + s23.l) + ((q0.l + q1.l) + (q2.l + q3.l)) + cross;
+                const float dn = (sn.h - 1.f) + c;  // sn.h - 1 is exact for sn.h in [1/2, 2]
+                if (!(fabsf(dn) < 1e-6f)) {
+                    renorm_bin_fp64(ph, pl, epad, e, (double)fh[e] + (double)fl[e], acc);
+                    continue;
+                }
+                const float corr = dn * fmaf(dn, .375f, -.5f);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const DF x = fast_two_sum(h[k], fmaf(h[k], corr, l[k]));
+                    h[k] = x.h;
+                    l[k] = x.l;
+                    ph[k * epad + e] = x.h;
+                    pl[k * epad + e] = x.l;
+                }
+                // density moments of the renormalised bin, weighted by fv
+                const DF a2 = df_dot2(h[0], l[0], h[0], l[0], h[1], l[1], h[1], l[1]);
+                const DF b2 = df_dot2(h[2], l[2], h[2], l[2], h[3], l[3], h[3], l[3]);
+                const DF r0 = df_add(a2, DF{-b2.h, -b2.l});
+                const DF r2 = df_dot2(h[0], l[0], h[2], l[2], h[1], l[1], h[3], l[3]);
+                const DF r3 = df_dot2(h[1], l[1], h[2], l[2], -h[0], -l[0], h[3], l[3]);
+                const DF fe{fh[e], fl[e]};
+                acc[0] = df_add(acc[0], df_mul(r0, fe));
+                acc[1] = df_add(acc[1], df_mul(r2, fe));
+                acc[2] = df_add(acc[2], df_mul(r3, fe));
             }
-            const double fe = fvp[e];
-            v[1] = fma((a[0] * a[0] + a[1] * a[1]) - (a[2] * a[2] + a[3] * a[3]), fe, v[1]);
-            v[2] = fma(a[0] * a[2] + a[1] * a[3], fe, v[2]);
-            v[3] = fma(a[1] * a[2] - a[0] * a[3], fe, v[3]);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) v[k + 1] = (double)acc[k].h + (double)acc[k].l;
         }
         v[1] *= .5;
         warp_reduce_scatter<4>(v, lane);
