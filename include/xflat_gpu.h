@@ -84,7 +84,8 @@ typedef struct xf_run_opts {
     long max_iters;        /* < 0: use cfg.Ts */
     int device_control;    /* 1: accept/reject and dr control run on the GPU, no per-step host sync */
     int iters_per_launch;  /* device_control: iterations captured per CUDA graph launch (default 16) */
-    int write_files;       /* 1: honour dump_mode through the NetCDF writer (host-driven loop only) */
+    int write_files;       /* 1: honour dump_mode through the NetCDF writer; under device_control the
+                              dump triggers run on the GPU and the state is staged there (same files) */
     int time_phases;       /* 1: time every phase kernel with CUDA events (see xf_phase_times) */
     double r0, dr0;        /* starting radius and step; NaN -> cfg.R0 / cfg.dr */
     double* log;           /* optional host buffer for accepted steps (itr, r_after, dr_used) */

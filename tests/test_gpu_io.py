@@ -132,3 +132,45 @@ def test_async_records_equal_states_of_each_accepted_step(tmp_path, precision, i
     for k in range(len(states)):
         assert np.array_equal(psi[k].reshape(states[k].shape), states[k]), k
         np.testing.assert_array_equal(prob[k].reshape(-1, 4), surv[k].reshape(-1, 4))
+
+
+def _files(tmp_path, text, device, iters, k=5):
+    sim = xg.Simulation(xg.Config.from_text(text))
+    o = xg._abi.XfRunOpts()
+    sim.lib.xf_run_opts_default(o)
+    o.max_iters = iters
+    o.write_files = 1
+    o.device_control = 1 if device else 0
+    o.iters_per_launch = k
+    st = xg._abi.XfRunStats()
+    assert sim.lib.xf_run(sim.h, o, xg._abi.XF_STEP_CB(0), None, st) == 0, sim.lib.xf_last_error(sim.h)
+    assert sim.lib.xf_io_close(sim.h) == 0
+    out = {}
+    for name in sorted(os.listdir(tmp_path)):
+        with scipy_io.netcdf_file(str(tmp_path / name), "r", mmap=False) as f:
+            out[name] = {v: f.variables[v][:].copy() for v in f.variables}
+    return out, st, sim.get_state(0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_control_writes_the_host_loops_files(tmp_path, precision):
+    """Under device control the step controller evaluates the dump triggers
+    and phase A stages the records: the files equal, record for record, those
+    of the host-driven loop (radius and iteration triggers, both kinds,
+    rotation every 4 Snapshot records, sync, a record decided at the last
+    step, several graph launches)."""
+    over = dict(dumpMode=3, r_step1="2.5e-5", r_step2="1e-5", itr_step1=7, newFile_step=4, sync_step=3,
+                t_step1=300000, t_step2=300000, Abins=12, Ebins=24)
+    a_dir, b_dir = tmp_path / "host", tmp_path / "dev"
+    a_dir.mkdir()
+    b_dir.mkdir()
+    ta = _cfg(a_dir, **over).replace("precision= fp64", "precision= " + precision)
+    tb = _cfg(b_dir, **over).replace("precision= fp64", "precision= " + precision)
+    fa, sa, pa = _files(a_dir, ta, False, 61)
+    fb, sb, pb = _files(b_dir, tb, True, 61)
+    assert (sa.iterations, sa.accepted) == (sb.iterations, sb.accepted)
+    assert np.array_equal(pa, pb)
+    assert list(fa) == list(fb) and len(fa) >= 4
+    for name in fa:
+        for v in fa[name]:
+            assert np.array_equal(fa[name][v], fb[name][v]), (name, v)

@@ -259,6 +259,136 @@ __device__ inline bool group_reduce(const RedTarget& rt, int G, int nused, const
 // J0 <- JC, record the step), count the iteration, update dr with the
 // reference's formula and clamps, and decide whether the loop ends.  Returns
 // true when the step was accepted.
+// The 8 bytes of v in reverse order: the halves swapped, each byte-reversed
+// (a double in the NetCDF file's big-endian encoding on a little-endian GPU).
+__device__ __forceinline__ double byte_reversed(double v)
+{
+    const unsigned lo = (unsigned)__double2loint(v), hi = (unsigned)__double2hiint(v);
+    return __hiloint2double((int)__byte_perm(lo, 0, 0x0123), (int)__byte_perm(hi, 0, 0x0123));
+}
+
+// Staging of one beam of psi0 for a record decided by the step controller
+// (one warp): the Snapshot slot receives the beam's four components, unpadded
+// and big-endian; the Probability slot its survival sum_e fv (ar^2 + ai^2)
+// with the spectrum of particle p % 2 (src/IO_f.cpp:341-351), reduced in the
+// order of the stand-alone output kernels so both routes write the same
+// bits.  psi is the FP64 state, or null for the compensated pair (hi, lo).
+__device__ inline void stage_beam(const Dev& d, const Ctl* ctl, int kind, int b, int lane, const double* psi,
+                                  const float* hi, const float* lo)
+{
+    const int epad = d.epad, ne = d.ne;
+    const size_t base = (size_t)b * 4 * epad;
+    if (kind & 1) {
+        double* dst = ctl->io_snap + (size_t)ctl->stage_snap_slot * ((size_t)d.nbeams * 4 * ne) + (size_t)b * 4 * ne;
+        for (int k = 0; k < 4; ++k)
+            for (int e = lane; e < ne; e += 32) {
+                const size_t i = base + (size_t)k * epad + e;
+                const double v = psi ? psi[i] : (double)hi[i] + (double)lo[i];
+                dst[(size_t)k * ne + e] = byte_reversed(v);
+            }
+    }
+    if (kind & 2) {
+        const double* fv = d.fv + (size_t)((b & 3) % 2) * epad;
+        double s = 0.;
+        for (int e = lane; e < epad; e += 32) {
+            double ar, ai;
+            if (psi) {
+                ar = psi[base + e];
+                ai = psi[base + epad + e];
+            } else {
+                ar = (double)hi[base + e] + (double)lo[base + e];
+                ai = (double)hi[base + epad + e] + (double)lo[base + epad + e];
+            }
+            s = fma(ar * ar + ai * ai, fv[e], s);
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
+        if (lane == 0) ctl->io_prob[(size_t)ctl->stage_prob_slot * d.nbeams + b] = s;
+    }
+}
+
+// After the last block of a phase A that staged a record: the record's slots
+// are complete.
+__device__ __forceinline__ void stage_done(Ctl* ctl)
+{
+    if (threadIdx.x == 0 && ctl->stage_kind) {
+        ctl->io_staged = ctl->io_count;
+        ctl->stage_kind = 0;
+    }
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The dump triggers of io_f::dumpToFile (src/IO_f.cpp:387-424) at an accepted
+// step (itr = counter_tot, r after the step, dr used), on the device.  The
+// radius and iteration triggers are exact; the wall-time triggers use the GPU
+// global timer in whole seconds since the last record, as the reference's
+// tv_sec differences do.  File rotation (src/IO_f.cpp:275-279) resets the
+// radius and time triggers to R0 and now, as io_f::init does.  A fired dump
+// becomes an IoRec and a staging request for the next phase A.
+__device__ inline void io_triggers(const Dev& d, Ctl* ctl, double r, double dr, long long itr)
+{
+    const unsigned long long now = globaltimer_ns();
+    if (!ctl->io_tinit) {
+        ctl->io_t1 = now - (unsigned long long)ctl->io_age1 * 1000000000ull;
+        ctl->io_t2 = now - (unsigned long long)ctl->io_age2 * 1000000000ull;
+        ctl->io_tinit = 1;
+    }
+    ctl->io_gt = now;
+    IoRec rec;
+    rec.r = r;
+    rec.dr = dr;
+    rec.itr = itr;
+    rec.kind = 0;
+    rec.snap_slot = rec.prob_slot = -1;
+    rec.rotate = rec.sync_snap = rec.sync_prob = 0;
+    if (ctl->io_mode & 1) {
+        const long long el = (long long)((now - ctl->io_t1) / 1000000000ull);
+        if (r == d.Rn || r - ctl->io_last_r1 > ctl->io_rstep1 || el > ctl->io_tstep1 ||
+            (ctl->io_itrstep1 > 0 && !(itr % ctl->io_itrstep1))) {
+            ctl->io_last_r1 = r;
+            ctl->io_t1 = now;
+            if (ctl->io_file_itr >= ctl->io_new_file_step) {
+                rec.rotate = 1;
+                ctl->io_file_itr = 0;
+                ctl->io_last_r1 = ctl->io_R0;
+                ctl->io_t1 = now;
+                if (ctl->io_mode & 2) {
+                    ctl->io_last_r2 = ctl->io_R0;
+                    ctl->io_t2 = now;
+                }
+            }
+            ctl->io_file_itr++;
+            rec.kind |= 1;
+            rec.snap_slot = (int)(ctl->io_snaps++ % ctl->io_nslots);
+            rec.sync_snap = ctl->io_sync_step > 0 && ctl->io_file_itr % ctl->io_sync_step == 0;
+        }
+    }
+    if (ctl->io_mode & 2) {
+        const long long el = (long long)((now - ctl->io_t2) / 1000000000ull);
+        if (r == d.Rn || r - ctl->io_last_r2 > ctl->io_rstep2 || el > ctl->io_tstep2 ||
+            (ctl->io_itrstep2 > 0 && !(itr % ctl->io_itrstep2))) {
+            ctl->io_last_r2 = r;
+            ctl->io_t2 = now;
+            rec.kind |= 2;
+            rec.prob_slot = (int)(ctl->io_probs++ % ctl->io_nslots);
+            rec.sync_prob = ctl->io_sync_step > 0 && ctl->io_file_itr % ctl->io_sync_step == 0;
+        }
+    }
+    if (rec.kind) {
+        ctl->io_log[ctl->io_count % ctl->io_log_cap] = rec;
+        ctl->io_count++;
+        ctl->stage_kind = rec.kind;
+        ctl->stage_snap_slot = rec.snap_slot;
+        ctl->stage_prob_slot = rec.prob_slot;
+    }
+}
+
 __device__ inline bool step_control(const Dev& d, Ctl* ctl, double me)
 {
     double r = ctl->r, dr = ctl->dr;
@@ -282,6 +412,7 @@ __device__ inline bool step_control(const Dev& d, Ctl* ctl, double me)
         }
         ctl->accepted++;
         acc = true;
+        if (ctl->io_mode) io_triggers(d, ctl, r, dr, ctl->iters);
     }
     ctl->iters++;
     dr *= d.ksi * sqrt(d.eps0 / me);

@@ -24,6 +24,18 @@ constexpr int kPartStride = 32;  // doubles per block in the partial-sum buffer
 
 enum Phase { PH_A = 0, PH_B = 1, PH_C = 2, PH_MOM = 3 };
 
+// One output record decided on the device by the step controller (the dump
+// triggers of src/IO_f.cpp:387-424 evaluated at an accepted step); the host
+// writes it once the following phase A has staged the state into its slots.
+struct IoRec {
+    double r, dr;
+    long long itr;
+    int kind;             // bit 1: Snapshot record, bit 2: Probability record
+    int snap_slot, prob_slot;
+    int rotate;           // the Snapshot record starts a new pair of files (src/IO_f.cpp:275-279)
+    int sync_snap, sync_prob;
+};
+
 struct Ctl {
     double r, dr;         // current iteration
     double hm[3];         // matter term at r, r+dr/2, r+dr
@@ -50,6 +62,31 @@ struct Ctl {
     long long max_iters;  // Ts
     long long log_len;    // accepted-step records written to the log
     int renorm_due;       // mixed precision: the last accepted step calls for a renormalisation
+    // device-side output (device control with files): trigger state of
+    // src/IO_f.cpp:387-424, record counters and the staging request
+    double io_last_r1, io_last_r2;
+    unsigned long long io_t1, io_t2;  // globaltimer (ns) of the last Snapshot / Probability record
+    long long io_age1, io_age2;       // seconds since those records when the run started
+    long long io_file_itr;            // records in the current Snapshot file
+    long long io_count;               // records decided
+    long long io_staged;              // records whose slots are filled
+    long long io_snaps, io_probs;     // slots handed out per kind (ring positions)
+    unsigned long long io_gt;         // globaltimer at the last evaluation
+    int io_tinit;                     // io_t1/io_t2 set from the ages
+    int stage_kind;                   // phase A stages psi0 (bit 1) / the survival (bit 2)
+    int stage_snap_slot, stage_prob_slot;
+    // device-side output configuration for the current run (io_mode 0: none);
+    // a per-run setting, kept here rather than in the kernel parameters so the
+    // cached CUDA graphs serve runs with and without files
+    int io_mode;                      // dumpMode bits
+    int io_nslots;
+    double io_R0, io_rstep1, io_rstep2;
+    long long io_tstep1, io_tstep2;   // seconds
+    long long io_itrstep1, io_itrstep2, io_new_file_step, io_sync_step;
+    double* io_snap;                  // [nslots][nbeams][4][ne] big-endian doubles (the file's encoding)
+    double* io_prob;                  // [nslots][nbeams] survival
+    IoRec* io_log;                    // [io_log_cap] ring of records
+    long long io_log_cap;
 };
 
 // Kernel parameters (passed by value).

@@ -459,7 +459,7 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
 // Prepares the control block for a device-controlled loop from (r, dr) with
 // an iteration budget Ts: moments of psi0 at stage point 0 of r, counters
 // reset, done set if there is nothing to do.  Synchronous.
-int xf_handle::start_device_run(double r, double dr, long Ts)
+int xf_handle::start_device_run(double r, double dr, long Ts, bool files)
 {
     int rc;
     if ((rc = push_inputs(r, dr))) return rc;
@@ -479,6 +479,9 @@ int xf_handle::start_device_run(double r, double dr, long Ts)
     h_ctl->renorm_due = 0;
     h_ctl->done = (r < cfg.Rn && Ts > 0) ? 0 : 1;
     for (int i = 0; i < 4; ++i) h_ctl->ticket[i] = 0;
+    h_ctl->io_mode = 0;
+    h_ctl->stage_kind = 0;
+    if (files) io_dev_fill(h_ctl);
     XF_CUDA(this, cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
     XF_CUDA(this, cudaStreamSynchronize(st));
     return XF_OK;
@@ -501,7 +504,9 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         if ((rc = dalloc(this, &d_log, 3 * (size_t)o.log_cap))) return rc;
         log_cap_dev = o.log_cap;
     }
-    if ((rc = start_device_run(r, dr, Ts))) return rc;
+    const bool files = o.write_files && cfg.dump_mode != 0;
+    if (files && (rc = io_dev_prepare(k))) return rc;
+    if ((rc = start_device_run(r, dr, Ts, files))) return rc;
     // instantiate the graph sizes this run needs before the timed region starts
     {
         cudaGraphExec_t ex;
@@ -519,8 +524,11 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         const int kk = (int)std::min<long long>(k, std::max<long long>(1, left));
         cudaGraphExec_t ex;
         if ((rc = get_graph(kk, o.time_phases != 0, &ex))) return rc;
+        // every iteration of the launch may decide an output record: their slots must be free
+        if (files && (rc = io_dev_reserve(kk))) return rc;
         XF_CUDA(this, cudaGraphLaunch(ex, st));
         XF_CUDA(this, cudaStreamSynchronize(st));
+        if (files && (rc = io_dev_drain(false))) return rc;
         const long long ran = h_ctl->iters - prev_iters;
         launches += 4 * ran;
         if (o.time_phases) {
@@ -539,6 +547,12 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     XF_CUDA(this, cudaEventSynchronize(ev[5]));
     float ms = 0.f;
     XF_CUDA(this, cudaEventElapsedTime(&ms, ev[4], ev[5]));
+    if (files) {
+        // the record of the last accepted step (if any) is staged here; then
+        // the trigger state returns to the host and the files are flushed
+        if ((rc = io_dev_drain(true))) return rc;
+        if ((rc = io_dev_end())) return rc;
+    }
     s.device_ms = ms;
     s.seconds = now_s() - t0;
     s.iterations = (long)h_ctl->iters;
@@ -760,7 +774,6 @@ int xf_run(xf_handle* h, const xf_run_opts* opts, xf_step_cb cb, void* user, xf_
     }
     int rc;
     if (o.device_control) {
-        if (o.write_files) return h->fail(XF_EUNSUPPORTED, "file output needs the host-driven loop");
         if (cb) return h->fail(XF_EUNSUPPORTED, "per-step callbacks need the host-driven loop");
         rc = h->run_device(o, s);
     } else {

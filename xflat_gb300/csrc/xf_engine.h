@@ -83,8 +83,16 @@ struct xf_handle {
     int accept();
     int run_host(const xf_run_opts& o, xf_step_cb cb, void* user, xf_run_stats& s);
     int run_device(const xf_run_opts& o, xf_run_stats& s);
-    int start_device_run(double r, double dr, long Ts);
+    int start_device_run(double r, double dr, long Ts, bool files = false);
     int get_graph(int k, bool timed, cudaGraphExec_t* out);
     int dump_files(long itr, double r, double dr);
     int flush_files();  // waits until every queued output record is written
+    // Device-controlled runs with files (xf_io.cpp): slots and files before the
+    // run, the per-run output fields of the control block, slot reservation
+    // before each graph launch, the records of each launch, and the end of the run.
+    int io_dev_prepare(int k);
+    void io_dev_fill(xf::Ctl* hc);
+    int io_dev_reserve(int k);
+    int io_dev_drain(bool final);
+    int io_dev_end();
 };

@@ -144,8 +144,10 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = 0.;
     const int myv = lane >> 2;  // value slot owned after an 8-way reduce-scatter
+    const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
+        if (stage) stage_beam(d, ctl, stage, b, lane, psi0, nullptr, nullptr);
         // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
         double sv = 0.;
         if (lane < 3) sv = beam_offset_k<GEOM>(d, ctl->J0, 0, hm, bi, lane);
@@ -187,6 +189,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         else if (myv < 6) add_moment<GEOM>(d, v[0], comp_of(myv - 3), 1, bi, acc);
     }
     if (!group_reduce<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
+    stage_done(ctl);
     if (threadIdx.x < kNJ) {
         ctl->JA1[threadIdx.x] = 0.;
         ctl->JA3[threadIdx.x] = 0.;

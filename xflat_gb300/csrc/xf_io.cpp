@@ -16,6 +16,14 @@
 // synchronous, so their errors are reported by the dump that triggers them;
 // an append error is reported by the next dump, xf_io_close or the end of
 // xf_run.
+//
+// Under device control the step controller itself evaluates the triggers at
+// every accepted step and logs a record; the next phase A stages psi0 and the
+// survival into a ring of device slots while it reads psi0 anyway.  Between
+// graph launches the host hands the staged records to the same copy stream
+// and writer thread, and before each launch it makes sure that the slots the
+// launch may fill have been copied out.  Records, their order, rotation and
+// sync are those of the host-driven loop.
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
@@ -76,6 +84,15 @@ struct xf_io {
     bool working = false, stop = false;
     int werr = 0;
     std::string werr_msg;
+
+    // device-controlled runs: slots the next phase A stages records into
+    int nslots = 0;
+    double* d_snapslots = nullptr;   // [nslots][nbeams][4][ne], big-endian
+    double* d_probslots = nullptr;   // [nslots][nbeams]
+    xf::IoRec* d_log = nullptr;      // [nslots] ring of records
+    std::vector<cudaEvent_t> snap_evt, prob_evt;  // last copy out of each slot
+    std::vector<char> snap_pend, prob_pend;
+    long long dev_done = 0;          // records of the current run handed to the writer
 };
 
 namespace {
@@ -232,6 +249,24 @@ int pipe_open(xf_handle* h)
     return XF_OK;
 }
 
+void slots_free(xf_io& io)
+{
+    if (io.d_snapslots) cudaFree(io.d_snapslots);
+    if (io.d_probslots) cudaFree(io.d_probslots);
+    if (io.d_log) cudaFree(io.d_log);
+    for (auto e : io.snap_evt)
+        if (e) cudaEventDestroy(e);
+    for (auto e : io.prob_evt)
+        if (e) cudaEventDestroy(e);
+    io.d_snapslots = io.d_probslots = nullptr;
+    io.d_log = nullptr;
+    io.snap_evt.clear();
+    io.prob_evt.clear();
+    io.snap_pend.clear();
+    io.prob_pend.clear();
+    io.nslots = 0;
+}
+
 void pipe_close(xf_io& io)
 {
     if (io.writer.joinable()) {
@@ -243,6 +278,7 @@ void pipe_close(xf_io& io)
         io.writer.join();
     }
     if (io.cs) cudaStreamSynchronize(io.cs);
+    slots_free(io);
     for (int i = 0; i < 2; ++i) {
         if (io.h_state[i]) cudaFreeHost(io.h_state[i]);
         if (io.h_surv[i]) cudaFreeHost(io.h_surv[i]);
@@ -406,6 +442,165 @@ int write_probability(xf_handle* h, double r)
 }  // namespace
 
 int xf_handle::dump_files(long it, double r, double dr) { return xf_dump(this, it, r, dr); }
+
+// ---------------------------------------------------------------- device-controlled runs
+
+int xf_handle::io_dev_prepare(int k)
+{
+    if (!io) io = new xf_io();
+    int rc;
+    if (!io->inited && (rc = io_init(this, 0))) return rc;
+    if ((rc = pipe_open(this))) return rc;
+    const int ns = k + 2;  // one launch's records, the record still waiting for its phase A, one spare
+    if (io->nslots != ns) {
+        if ((rc = drain(this))) return rc;
+        cudaStreamSynchronize(io->cs);
+        slots_free(*io);
+        const size_t snap = (size_t)nbeams * 4 * ne;
+        cudaError_t e = cudaSuccess;
+        if (cfg.dump_mode & 1) e = cudaMalloc((void**)&io->d_snapslots, ns * snap * sizeof(double));
+        if (e == cudaSuccess && (cfg.dump_mode & 2))
+            e = cudaMalloc((void**)&io->d_probslots, ns * (size_t)nbeams * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&io->d_log, ns * sizeof(xf::IoRec));
+        io->snap_evt.assign(ns, nullptr);
+        io->prob_evt.assign(ns, nullptr);
+        for (int i = 0; i < ns && e == cudaSuccess; ++i) {
+            e = cudaEventCreateWithFlags(&io->snap_evt[i], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&io->prob_evt[i], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) {
+            slots_free(*io);
+            return fail(XF_ENOMEM, std::string("output slots: ") + cudaGetErrorString(e));
+        }
+        io->snap_pend.assign(ns, 0);
+        io->prob_pend.assign(ns, 0);
+        io->nslots = ns;
+    }
+    io->dev_done = 0;
+    return XF_OK;
+}
+
+void xf_handle::io_dev_fill(xf::Ctl* hc)
+{
+    const xf_config& c = cfg;
+    const long now = wall_s();
+    hc->io_mode = c.dump_mode;
+    hc->io_nslots = io->nslots;
+    hc->io_R0 = c.R0;
+    hc->io_rstep1 = c.rstep1;
+    hc->io_rstep2 = c.rstep2;
+    hc->io_tstep1 = c.tstep1;
+    hc->io_tstep2 = c.tstep2;
+    hc->io_itrstep1 = c.itrstep1;
+    hc->io_itrstep2 = c.itrstep2;
+    hc->io_new_file_step = c.new_file_step;
+    hc->io_sync_step = c.sync_step;
+    hc->io_snap = io->d_snapslots;
+    hc->io_prob = io->d_probslots;
+    hc->io_log = io->d_log;
+    hc->io_log_cap = io->nslots;
+    hc->io_last_r1 = io->last_r1;
+    hc->io_last_r2 = io->last_r2;
+    hc->io_age1 = std::max(0L, now - io->t1);
+    hc->io_age2 = std::max(0L, now - io->t2);
+    hc->io_tinit = 0;
+    hc->io_file_itr = (long long)io->itr;
+    hc->io_count = hc->io_staged = hc->io_snaps = hc->io_probs = 0;
+    hc->stage_kind = 0;
+}
+
+int xf_handle::io_dev_reserve(int k)
+{
+    for (int i = 0; i < k; ++i) {
+        const int s = (int)((h_ctl->io_snaps + i) % io->nslots), p = (int)((h_ctl->io_probs + i) % io->nslots);
+        if (io->snap_pend[s]) {
+            if (cudaEventSynchronize(io->snap_evt[s]) != cudaSuccess) return fail(XF_ECUDA, "output slot copy failed");
+            io->snap_pend[s] = 0;
+        }
+        if (io->prob_pend[p]) {
+            if (cudaEventSynchronize(io->prob_evt[p]) != cudaSuccess) return fail(XF_ECUDA, "output slot copy failed");
+            io->prob_pend[p] = 0;
+        }
+    }
+    return XF_OK;
+}
+
+int xf_handle::io_dev_drain(bool final)
+{
+    int rc;
+    if (final && h_ctl->io_staged < h_ctl->io_count) {
+        // the run ended with the step that decided this record
+        xf::launch_stage_pending(dev, mixed != nullptr, st);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+            return fail(XF_ECUDA, "staging the last output record failed");
+        launches++;
+    }
+    const long long staged = final ? h_ctl->io_count : h_ctl->io_staged;
+    if (staged <= io->dev_done) return XF_OK;
+    std::vector<xf::IoRec> ring(io->nslots);
+    if (cudaMemcpy(ring.data(), io->d_log, ring.size() * sizeof(xf::IoRec), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(XF_ECUDA, "reading the output records failed");
+    const size_t snap = (size_t)nbeams * 4 * ne;
+    for (long long n = io->dev_done; n < staged; ++n) {
+        const xf::IoRec& rec = ring[n % io->nslots];
+        if (rec.rotate && (rc = io_init(this, io->ctr + 1))) return rc;
+        if (rec.kind & 1) {
+            if (io->verbose) std::printf("%f\n", rec.r);
+            const int b = io->next_state;
+            if ((rc = claim(this, io->busy_state, b))) return rc;
+            cudaError_t e = cudaMemcpyAsync(io->h_state[b], io->d_snapslots + rec.snap_slot * snap, snap * sizeof(double),
+                                            cudaMemcpyDeviceToHost, io->cs);
+            if (e == cudaSuccess) e = cudaEventRecord(io->state_copied[b], io->cs);
+            if (e == cudaSuccess) e = cudaEventRecord(io->snap_evt[rec.snap_slot], io->cs);
+            if (e != cudaSuccess) {
+                unclaim(*io, io->busy_state, b);
+                return fail(XF_ECUDA, std::string("output copy: ") + cudaGetErrorString(e));
+            }
+            io->snap_pend[rec.snap_slot] = 1;
+            io->itr++;
+            enqueue(*io, Job{JOB_SNAP, b, rec.r, rec.dr, rec.sync_snap != 0});
+            io->next_state ^= 1;
+        }
+        if (rec.kind & 2) {
+            if (io->verbose) std::printf("%f\n", rec.r);
+            const int b = io->next_surv;
+            if ((rc = claim(this, io->busy_surv, b))) return rc;
+            cudaError_t e = cudaMemcpyAsync(io->h_surv[b], io->d_probslots + (size_t)rec.prob_slot * nbeams,
+                                            (size_t)nbeams * sizeof(double), cudaMemcpyDeviceToHost, io->cs);
+            if (e == cudaSuccess) e = cudaEventRecord(io->surv_copied[b], io->cs);
+            if (e == cudaSuccess) e = cudaEventRecord(io->prob_evt[rec.prob_slot], io->cs);
+            if (e != cudaSuccess) {
+                unclaim(*io, io->busy_surv, b);
+                return fail(XF_ECUDA, std::string("output copy: ") + cudaGetErrorString(e));
+            }
+            io->prob_pend[rec.prob_slot] = 1;
+            enqueue(*io, Job{JOB_PROB, b, rec.r, 0., rec.sync_prob != 0});
+            io->next_surv ^= 1;
+        }
+    }
+    io->dev_done = staged;
+    return XF_OK;
+}
+
+int xf_handle::io_dev_end()
+{
+    int rc;
+    if ((rc = pull_ctl())) return rc;
+    // the trigger state continues on the host (a later host-driven run or xf_dump)
+    io->last_r1 = h_ctl->io_last_r1;
+    io->last_r2 = h_ctl->io_last_r2;
+    if (h_ctl->io_tinit) {
+        const long now = wall_s();
+        io->t1 = now - (long)((h_ctl->io_gt - h_ctl->io_t1) / 1000000000ull);
+        io->t2 = now - (long)((h_ctl->io_gt - h_ctl->io_t2) / 1000000000ull);
+    }
+    h_ctl->io_mode = 0;
+    h_ctl->stage_kind = 0;
+    if (cudaMemcpyAsync(d_ctl, h_ctl, sizeof(xf::Ctl), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return fail(XF_ECUDA, "control block upload failed");
+    return flush_files();
+}
 
 // Drains the writer and flushes both files (records and the header's record
 // count), so another reader sees every record written so far.

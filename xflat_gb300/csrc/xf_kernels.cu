@@ -137,13 +137,6 @@ __global__ void k_hvv_eval(Dev d, const double* __restrict__ J, int pt, double* 
     hvv[4 * i + 3] = H[2];
 }
 
-// The 8 bytes of v in reverse order: the halves swapped, each byte-reversed.
-__device__ __forceinline__ double byte_reversed(double v)
-{
-    const unsigned lo = (unsigned)__double2loint(v), hi = (unsigned)__double2hiint(v);
-    return __hiloint2double((int)__byte_perm(lo, 0, 0x0123), (int)__byte_perm(hi, 0, 0x0123));
-}
-
 // Reads psi0 through the control block, so the copy follows the role swaps of
 // accepted steps without a host round trip.
 __global__ void k_stage_state(Dev d, int mixed, int big_endian, double* __restrict__ dst)
@@ -187,6 +180,19 @@ __global__ void k_survival(Dev d, int mixed, double* __restrict__ out)
         for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
         if (lane == 0) out[b] = s;
     }
+}
+
+// A record decided at the last accepted step of a device-controlled run has
+// no following phase A to stage it: the same staging, one warp per beam.
+__global__ void k_stage_pending(Dev d, int mixed)
+{
+    const Ctl* ctl = d.ctl;
+    const int kind = ctl->stage_kind;
+    if (!kind) return;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < d.nbeams; b += nw)
+        stage_beam(d, ctl, kind, b, lane, mixed ? nullptr : ctl->psi0, ctl->m0hi, ctl->m0lo);
 }
 
 }  // namespace
@@ -244,6 +250,11 @@ void launch_accept(const Dev& d, cudaStream_t st) { k_accept<<<1, 1, 0, st>>>(d)
 void launch_stage_state(const Dev& d, int mixed, int big_endian, double* dst, cudaStream_t st)
 {
     k_stage_state<<<152 * 4, 256, 0, st>>>(d, mixed, big_endian, dst);
+}
+
+void launch_stage_pending(const Dev& d, int mixed, cudaStream_t st)
+{
+    k_stage_pending<<<max_phase_blocks(d.nbeams, 256), 256, 0, st>>>(d, mixed);
 }
 
 void launch_survival(const Dev& d, int mixed, double* out, cudaStream_t st)

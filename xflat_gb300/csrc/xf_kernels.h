@@ -30,5 +30,8 @@ void launch_stage_state(const Dev& d, int mixed, int big_endian, double* dst, cu
 // Per-beam survival sum_e fv (ar^2 + ai^2) of psi0 (the Probability file's
 // quantity, src/IO_f.cpp:341-351), out[nbeams].
 void launch_survival(const Dev& d, int mixed, double* out, cudaStream_t st);
+// Stages the output record the step controller decided last, if its phase A
+// did not run (the run ended with that step).
+void launch_stage_pending(const Dev& d, int mixed, cudaStream_t st);
 
 }  // namespace xf

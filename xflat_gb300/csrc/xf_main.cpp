@@ -41,7 +41,7 @@ int main(int argc, char** argv)
     }
     // with files to write the loop is host-driven; otherwise the step control runs on the GPU
     o.write_files = cfg.dump_mode != 0;
-    o.device_control = cfg.dump_mode == 0;
+    o.device_control = 1;  // triggers and staging on the device, files written between graph launches
     xf_io_verbose(h, 1);
     xf_run_stats s;
     rc = xf_run(h, &o, nullptr, nullptr, &s);

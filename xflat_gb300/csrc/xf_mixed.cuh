@@ -314,8 +314,10 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] = 0.;
     const int myv = lane >> 2;
+    const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
+        if (stage) stage_beam(d, ctl, stage, b, lane, nullptr, ctl->m0hi, ctl->m0lo);
         // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
         float sv = 0.f;
         if (lane < 3) sv = (float)beam_offset_k<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi, lane);
@@ -362,6 +364,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         else if (myv < 6) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv - 3), v[0]), comp_of(myv - 3), 1, bi, acc);
     }
     if (!group_reduce<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
+    stage_done(ctl);
     if (threadIdx.x < kNJ) {
         ctl->JA1[threadIdx.x] = 0.;
         ctl->JA3[threadIdx.x] = 0.;
