@@ -516,6 +516,8 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     const double t0 = now_s();
     XF_CUDA(this, cudaEventRecord(ev[4], st));
     long long prev_iters = 0;
+    long long io_count = 0, io_staged = 0;  // records of the previous launch, drained during the next
+    bool io_pending = false;
     while (!h_ctl->done) {
         if ((long)(now_s() - t0) >= cfg.Tn) break;
         // the last launch is sized to the remaining iteration budget, so that no
@@ -527,8 +529,15 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         // every iteration of the launch may decide an output record: their slots must be free
         if (files && (rc = io_dev_reserve(kk))) return rc;
         XF_CUDA(this, cudaGraphLaunch(ex, st));
+        // the previous launch's records go to the writer while this launch runs
+        if (io_pending && (rc = io_dev_drain(io_count, io_staged, false))) return rc;
+        io_pending = false;
         XF_CUDA(this, cudaStreamSynchronize(st));
-        if (files && (rc = io_dev_drain(false))) return rc;
+        if (files) {
+            io_count = h_ctl->io_count;
+            io_staged = h_ctl->io_staged;
+            io_pending = true;
+        }
         const long long ran = h_ctl->iters - prev_iters;
         launches += 4 * ran;
         if (o.time_phases) {
@@ -550,7 +559,7 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     if (files) {
         // the record of the last accepted step (if any) is staged here; then
         // the trigger state returns to the host and the files are flushed
-        if ((rc = io_dev_drain(true))) return rc;
+        if ((rc = io_dev_drain(h_ctl->io_count, h_ctl->io_staged, true))) return rc;
         if ((rc = io_dev_end())) return rc;
     }
     s.device_ms = ms;

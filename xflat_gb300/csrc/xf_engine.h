@@ -93,6 +93,6 @@ struct xf_handle {
     int io_dev_prepare(int k);
     void io_dev_fill(xf::Ctl* hc);
     int io_dev_reserve(int k);
-    int io_dev_drain(bool final);
+    int io_dev_drain(long long count, long long staged, bool final);
     int io_dev_end();
 };

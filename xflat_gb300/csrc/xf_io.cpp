@@ -44,6 +44,11 @@ namespace {
 
 enum { JOB_SNAP = 0, JOB_PROB = 1 };
 
+// Pinned host buffers per record kind: two for the (large) Snapshot records,
+// many for the (small) Probability records, so that a burst of the latter does
+// not wait for the writer.
+constexpr int kStateBufs = 2, kSurvBufs = 32;
+
 struct Job {
     int kind;
     int buf;
@@ -68,10 +73,10 @@ struct xf_io {
     cudaStream_t cs = nullptr;                // copy stream
     double* d_state = nullptr;                // staged psi0, padded layout, big-endian
     double* d_surv = nullptr;                 // staged survival, [nbeams]
-    double* h_state[2] = {nullptr, nullptr};  // pinned, unpadded [beam][comp][ebin], big-endian
-    double* h_surv[2] = {nullptr, nullptr};
+    double* h_state[kStateBufs] = {};         // pinned, unpadded [beam][comp][ebin], big-endian
+    double* h_surv[kSurvBufs] = {};
     cudaEvent_t staged = nullptr;             // compute stream: staging kernel done
-    cudaEvent_t state_copied[2] = {nullptr, nullptr}, surv_copied[2] = {nullptr, nullptr};
+    cudaEvent_t state_copied[kStateBufs] = {}, surv_copied[kSurvBufs] = {};
     cudaEvent_t state_d2h = nullptr, surv_d2h = nullptr;  // last copy out of each staging buffer
     bool state_d2h_pending = false, surv_d2h_pending = false;
     int next_state = 0, next_surv = 0;
@@ -80,7 +85,7 @@ struct xf_io {
     std::mutex mu;
     std::condition_variable cv;
     std::deque<Job> q;
-    bool busy_state[2] = {false, false}, busy_surv[2] = {false, false};
+    bool busy_state[kStateBufs] = {}, busy_surv[kSurvBufs] = {};
     bool working = false, stop = false;
     int werr = 0;
     std::string werr_msg;
@@ -233,11 +238,13 @@ int pipe_open(xf_handle* h)
     if ((rc = ck(cudaStreamCreateWithFlags(&io.cs, cudaStreamNonBlocking), "copy stream"))) return rc;
     if ((rc = ck(cudaMalloc((void**)&io.d_state, padded * sizeof(double)), "cudaMalloc"))) return rc;
     if ((rc = ck(cudaMalloc((void**)&io.d_surv, (size_t)h->nbeams * sizeof(double)), "cudaMalloc"))) return rc;
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kStateBufs; ++i) {
         if ((rc = ck(cudaMallocHost((void**)&io.h_state[i], plain * sizeof(double)), "cudaMallocHost"))) return rc;
+        if ((rc = ck(cudaEventCreateWithFlags(&io.state_copied[i], cudaEventDisableTiming), "event"))) return rc;
+    }
+    for (int i = 0; i < kSurvBufs; ++i) {
         if ((rc = ck(cudaMallocHost((void**)&io.h_surv[i], (size_t)h->nbeams * sizeof(double)), "cudaMallocHost")))
             return rc;
-        if ((rc = ck(cudaEventCreateWithFlags(&io.state_copied[i], cudaEventDisableTiming), "event"))) return rc;
         if ((rc = ck(cudaEventCreateWithFlags(&io.surv_copied[i], cudaEventDisableTiming), "event"))) return rc;
     }
     if ((rc = ck(cudaEventCreateWithFlags(&io.staged, cudaEventDisableTiming), "event"))) return rc;
@@ -279,13 +286,17 @@ void pipe_close(xf_io& io)
     }
     if (io.cs) cudaStreamSynchronize(io.cs);
     slots_free(io);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kStateBufs; ++i) {
         if (io.h_state[i]) cudaFreeHost(io.h_state[i]);
-        if (io.h_surv[i]) cudaFreeHost(io.h_surv[i]);
         if (io.state_copied[i]) cudaEventDestroy(io.state_copied[i]);
+        io.h_state[i] = nullptr;
+        io.state_copied[i] = nullptr;
+    }
+    for (int i = 0; i < kSurvBufs; ++i) {
+        if (io.h_surv[i]) cudaFreeHost(io.h_surv[i]);
         if (io.surv_copied[i]) cudaEventDestroy(io.surv_copied[i]);
-        io.h_state[i] = io.h_surv[i] = nullptr;
-        io.state_copied[i] = io.surv_copied[i] = nullptr;
+        io.h_surv[i] = nullptr;
+        io.surv_copied[i] = nullptr;
     }
     if (io.d_state) cudaFree(io.d_state);
     if (io.d_surv) cudaFree(io.d_surv);
@@ -410,7 +421,7 @@ int write_snapshot(xf_handle* h, double r, double dr)
     }
     io.itr++;
     enqueue(io, Job{JOB_SNAP, b, r, dr, c.sync_step > 0 && io.itr % c.sync_step == 0});
-    io.next_state ^= 1;
+    io.next_state = (io.next_state + 1) % kStateBufs;
     return XF_OK;
 }
 
@@ -435,7 +446,7 @@ int write_probability(xf_handle* h, double r)
     }
     const int64_t ss = h->cfg.sync_step;
     enqueue(io, Job{JOB_PROB, b, r, 0., ss > 0 && io.itr % ss == 0});
-    io.next_surv ^= 1;
+    io.next_surv = (io.next_surv + 1) % kSurvBufs;
     return XF_OK;
 }
 
@@ -451,7 +462,9 @@ int xf_handle::io_dev_prepare(int k)
     int rc;
     if (!io->inited && (rc = io_init(this, 0))) return rc;
     if ((rc = pipe_open(this))) return rc;
-    const int ns = k + 2;  // one launch's records, the record still waiting for its phase A, one spare
+    // records of two launches (one being written while the next runs), the
+    // record still waiting for its phase A, one spare
+    const int ns = 2 * k + 2;
     if (io->nslots != ns) {
         if ((rc = drain(this))) return rc;
         cudaStreamSynchronize(io->cs);
@@ -525,17 +538,17 @@ int xf_handle::io_dev_reserve(int k)
     return XF_OK;
 }
 
-int xf_handle::io_dev_drain(bool final)
+int xf_handle::io_dev_drain(long long count, long long staged_in, bool final)
 {
     int rc;
-    if (final && h_ctl->io_staged < h_ctl->io_count) {
+    if (final && staged_in < count) {
         // the run ended with the step that decided this record
         xf::launch_stage_pending(dev, mixed != nullptr, st);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
             return fail(XF_ECUDA, "staging the last output record failed");
         launches++;
     }
-    const long long staged = final ? h_ctl->io_count : h_ctl->io_staged;
+    const long long staged = final ? count : staged_in;
     if (staged <= io->dev_done) return XF_OK;
     std::vector<xf::IoRec> ring(io->nslots);
     if (cudaMemcpy(ring.data(), io->d_log, ring.size() * sizeof(xf::IoRec), cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -559,7 +572,7 @@ int xf_handle::io_dev_drain(bool final)
             io->snap_pend[rec.snap_slot] = 1;
             io->itr++;
             enqueue(*io, Job{JOB_SNAP, b, rec.r, rec.dr, rec.sync_snap != 0});
-            io->next_state ^= 1;
+            io->next_state = (io->next_state + 1) % kStateBufs;
         }
         if (rec.kind & 2) {
             if (io->verbose) std::printf("%f\n", rec.r);
@@ -575,7 +588,7 @@ int xf_handle::io_dev_drain(bool final)
             }
             io->prob_pend[rec.prob_slot] = 1;
             enqueue(*io, Job{JOB_PROB, b, rec.r, 0., rec.sync_prob != 0});
-            io->next_surv ^= 1;
+            io->next_surv = (io->next_surv + 1) % kSurvBufs;
         }
     }
     io->dev_done = staged;
