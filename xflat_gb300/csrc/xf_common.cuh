@@ -161,6 +161,35 @@ __device__ __forceinline__ void add_moment(const Dev& d, double val, int z, int 
     }
 }
 
+// The same contribution split over lanes: after a reduce-scatter the G lanes
+// of a value slot hold the same value, and lane k of the group accumulates
+// moment k alone (k < K; MA has 2 moments, MAA 4).  Each moment is formed as
+// ((c A) B) C with the factors chosen per lane, which repeats the operations
+// of add_moment exactly (the unused factors are 1), so the sums are the same
+// bits while the FP64 work per lane drops from all K moments to one.
+template <int GEOM>
+__device__ __forceinline__ void add_moment_lane(const Dev& d, double val, int z, int pt, const BeamIdx& bi, int k,
+                                                double& acc)
+{
+    if (k >= NK<GEOM>::K) return;
+    const double sgn = (z == 3 || (bi.p & 1) == 0) ? 1.0 : -1.0;
+    const double c = (val * le_of(d, bi.p)) * sgn;
+    const double dc = geo(d, 2, pt, bi.ang);
+    double A, B, C;
+    if (GEOM == 0 || k == 0 || k == 3) {
+        // c dc, or (c dc) cos
+        A = dc;
+        B = k == 0 ? 1.0 : geo(d, 0, pt, bi.ang);
+        C = 1.0;
+    } else {
+        // ((c cos(phi)) sin(theta)) dc and ((c sin(phi)) sin(theta)) dc
+        A = k == 1 ? d.cosphi[bi.phi] : d.sinphi[bi.phi];
+        B = geo(d, 1, pt, bi.ang);
+        C = dc;
+    }
+    acc += ((c * A) * B) * C;
+}
+
 // Value slot v of a phase -> (stage point, density component) of the moment it feeds.
 __device__ __forceinline__ int comp_of(int k) { return k == 0 ? 0 : (k == 1 ? 2 : 3); }
 
@@ -180,16 +209,40 @@ struct RedTarget {
 };
 
 template <int K>
+__device__ inline bool group_reduce_tail(const RedTarget& rt, int nused, double mx, bool with_max, double* s_warp,
+                                         double* s_out);
+
+template <int K>
 __device__ inline bool group_reduce(const RedTarget& rt, int G, int nused, const double (&acc)[K], double mx,
                                     bool with_max, double* s_warp, double* s_out)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int nout = nused * K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int v = lane / G;
     if ((lane % G) == 0 && v < nused) {
 #pragma unroll
         for (int k = 0; k < K; ++k) s_warp[warp * 32 + v * K + k] = acc[k];
     }
+    return group_reduce_tail<K>(rt, nused, mx, with_max, s_warp, s_out);
+}
+
+// group_reduce for lane-split accumulators (add_moment_lane): lane v G + k
+// holds moment k of value slot v.
+template <int K>
+__device__ inline bool group_reduce_split(const RedTarget& rt, int G, int nused, double acc, double mx, bool with_max,
+                                          double* s_warp, double* s_out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int v = lane / G, k = lane % G;
+    if (k < K && v < nused) s_warp[warp * 32 + v * K + k] = acc;
+    return group_reduce_tail<K>(rt, nused, mx, with_max, s_warp, s_out);
+}
+
+template <int K>
+__device__ inline bool group_reduce_tail(const RedTarget& rt, int nused, double mx, bool with_max, double* s_warp,
+                                         double* s_out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nout = nused * K;
     if (with_max && lane == 0) s_warp[warp * 32 + 31] = mx;
     __syncthreads();
     double* part = rt.partials + (size_t)rt.idx * kPartStride;

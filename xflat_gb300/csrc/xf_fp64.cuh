@@ -140,9 +140,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     const int myv = lane >> 2;  // value slot owned after an 8-way reduce-scatter
     const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
     for (int b = gw; b < d.nbeams; b += tw) {
@@ -185,10 +183,10 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         v[0] *= .5;
         v[3] *= .5;
         warp_reduce_scatter<8>(v, lane);
-        if (myv < 3) add_moment<GEOM>(d, v[0], comp_of(myv), 2, bi, acc);
-        else if (myv < 6) add_moment<GEOM>(d, v[0], comp_of(myv - 3), 1, bi, acc);
+        if (myv < 3) add_moment_lane<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 3, acc);
+        else if (myv < 6) add_moment_lane<GEOM>(d, v[0], comp_of(myv - 3), 1, bi, lane & 3, acc);
     }
-    if (!group_reduce<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
+    if (!group_reduce_split<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
     stage_done(ctl);
     if (threadIdx.x < kNJ) {
         ctl->JA1[threadIdx.x] = 0.;
@@ -220,9 +218,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
@@ -260,9 +256,9 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         }
         v[0] *= .5;
         warp_reduce_scatter<4>(v, lane);
-        if (myv < 3) add_moment<GEOM>(d, v[0], comp_of(myv), 2, bi, acc);
+        if (myv < 3) add_moment_lane<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 7, acc);
     }
-    if (!group_reduce<K>(rt, 8, 3, acc, 0., false, s_warp, s_out)) return;
+    if (!group_reduce_split<K>(rt, 8, 3, acc, 0., false, s_warp, s_out)) return;
     if (threadIdx.x < kNJ) ctl->JB4[threadIdx.x] = 0.;
     __syncthreads();
     if ((int)threadIdx.x < 3 * K) {
@@ -292,9 +288,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     double mx = -1.0;
     const int myv = lane >> 3;  // 0: error, 1..3: density components 0, 2, 3
     for (int b = gw; b < d.nbeams; b += tw) {
@@ -333,7 +327,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         v[1] *= .5;
         warp_reduce_scatter<4>(v, lane);
         if (myv == 0) mx = fmax(mx, v[0]);
-        else add_moment<GEOM>(d, v[0], comp_of(myv - 1), 2, bi, acc);
+        else add_moment_lane<GEOM>(d, v[0], comp_of(myv - 1), 2, bi, lane & 7, acc);
         // per-beam moments of the candidate (the reference's hSumMat of psi4)
         if ((lane & 7) == 0) {
             if (myv == 0) S4[(size_t)b * 4 + 1] = 0.;
@@ -341,10 +335,8 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         }
     }
     // lanes 8..31 hold moments of slots 1..3; shift them to slots 0..2 for the block reduction
-    double accs[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) accs[k] = __shfl_down_sync(kFull, acc[k], 8);
-    if (!group_reduce<K>(rt, 8, 3, accs, mx, true, s_warp, s_out)) return;
+    const double accs = __shfl_down_sync(kFull, acc, 8);
+    if (!group_reduce_split<K>(rt, 8, 3, accs, mx, true, s_warp, s_out)) return;
     if (threadIdx.x < kNJ) ctl->JC[threadIdx.x] = 0.;
     __syncthreads();
     if ((int)threadIdx.x < 3 * K) {

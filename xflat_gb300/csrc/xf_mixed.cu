@@ -52,23 +52,29 @@ using mixed::KSum;
 // The phase kernels are latency-bound (dependent FP32 chains and state loads,
 // one warp per beam); register caps that raise the resident warps per SM beat
 // the few spills they cause (measured on GB300 at 2048 x 4 x 512 bins: phase C
-// 0.165 ms at 2 blocks/SM, 0.119 ms at 4).
+// 0.165 ms at 2 blocks/SM, 0.119 ms at 4).  Minimum resident blocks per SM by
+// phase (A, B, C) and geometry (MA/SA, MAA).
+constexpr int mix_min_blocks(int phase, int geom)
+{
+    return geom == 0 ? (phase == 0 ? 5 : phase == 1 ? 6 : 4) : (phase == 0 ? 5 : phase == 1 ? 6 : 4);
+}
+
 template <int GEOM>
-__global__ void __launch_bounds__(256, 5) k_mixA(Dev d)
+__global__ void __launch_bounds__(256, mix_min_blocks(0, GEOM)) k_mixA(Dev d)
 {
     pdl_enter();
     mixed::phaseA_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_A));
 }
 
 template <int GEOM>
-__global__ void __launch_bounds__(256, 6) k_mixB(Dev d)
+__global__ void __launch_bounds__(256, mix_min_blocks(1, GEOM)) k_mixB(Dev d)
 {
     pdl_enter();
     mixed::phaseB_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_B));
 }
 
 template <int GEOM>
-__global__ void __launch_bounds__(256, 4) k_mixC(Dev d)
+__global__ void __launch_bounds__(256, mix_min_blocks(2, GEOM)) k_mixC(Dev d)
 {
     pdl_enter();
     mixed::phaseC_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_C));

@@ -294,6 +294,82 @@ __device__ __forceinline__ double stage_sum(const double* S0, int b, int comp, d
     return S0[(size_t)b * 4 + comp] + inc;
 }
 
+// ------------------------------------------------------------------ double-float
+
+// Error-free transformations on FP32 (the compensated pairs' arithmetic):
+// TwoSum (Knuth), Fast2Sum (Dekker, |a| >= |b|) and the FMA-based TwoProduct.
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ DF two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bp = s - a;
+    return DF{s, (a - (s - bp)) + (b - bp)};
+}
+
+__device__ __forceinline__ DF fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+
+__device__ __forceinline__ DF two_prod(float a, float b)
+{
+    const float p = a * b;
+    return DF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ DF df_add(const DF& a, const DF& b)
+{
+    const DF s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, s.l + (a.l + b.l));
+}
+
+__device__ __forceinline__ DF df_mul(const DF& a, const DF& b)
+{
+    const DF p = two_prod(a.h, b.h);
+    return fast_two_sum(p.h, fmaf(a.h, b.l, fmaf(a.l, b.h, p.l)));
+}
+
+// x0 x1 + y0 y1 for compensated pairs x = (x0 + xl0), ... (the lo*lo terms,
+// 2^-48 of the result, are dropped).
+__device__ __forceinline__ DF df_dot2(float x0, float xl0, float x1, float xl1, float y0, float yl0, float y1,
+                                      float yl1)
+{
+    const DF p = two_prod(x0, x1), q = two_prod(y0, y1);
+    const DF t = two_sum(p.h, q.h);
+    const float cross = fmaf(x0, xl1, fmaf(xl0, x1, fmaf(y0, yl1, yl0 * y1)));
+    return fast_two_sum(t.h, t.l + (p.l + q.l + cross));
+}
+
+// Warp reduce-scatter of NV double-float values (the FP32 counterpart of
+// warp_reduce_scatter, same exchange pattern): afterwards each group of
+// 32/NV lanes holds the warp total of one value.  Per-lane Kahan sums enter
+// as (s, -c); the totals keep about 2^-44 of their size, far below the FP32
+// precision of the increments they sum.
+template <int NV>
+__device__ __forceinline__ void df_reduce_scatter(DF (&v)[NV], int lane)
+{
+    int off = 16;
+#pragma unroll
+    for (int half = NV / 2; half >= 1; half >>= 1, off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const DF keep = upper ? v[i + half] : v[i];
+            const DF send = upper ? v[i] : v[i + half];
+            v[i] = df_add(keep, DF{__shfl_xor_sync(kFull, send.h, off), __shfl_xor_sync(kFull, send.l, off)});
+        }
+    }
+#pragma unroll
+    for (; off >= 1; off >>= 1)
+        v[0] = df_add(v[0], DF{__shfl_xor_sync(kFull, v[0].h, off), __shfl_xor_sync(kFull, v[0].l, off)});
+}
+
+__device__ __forceinline__ double df_value(const DF& x) { return (double)x.h + (double)x.l; }
+
 // ------------------------------------------------------------------ phase A
 
 // Moments of psi1 = U(h0, dl1) psi0 at point 2 and of psi3 = U(h0, dl0) psi0 at point 1.
@@ -310,9 +386,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     const int myv = lane >> 2;
     const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
     for (int b = gw; b < d.nbeams; b += tw) {
@@ -353,17 +427,19 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
             acc_drho(x, d1, f, s[0], s[1], s[2]);
             acc_drho(x, d3, f, s[3], s[4], s[5]);
         }
-        double v[8];
+        DF v[8];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) v[i] = s[i].value();
-        v[6] = v[7] = 0.;
-        v[0] *= .5;
-        v[3] *= .5;
-        warp_reduce_scatter<8>(v, lane);
-        if (myv < 3) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv), v[0]), comp_of(myv), 2, bi, acc);
-        else if (myv < 6) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv - 3), v[0]), comp_of(myv - 3), 1, bi, acc);
+        for (int i = 0; i < 6; ++i) v[i] = DF{s[i].s, -s[i].c};
+        v[6] = v[7] = DF{0.f, 0.f};
+        v[0] = DF{.5f * v[0].h, .5f * v[0].l};
+        v[3] = DF{.5f * v[3].h, .5f * v[3].l};
+        df_reduce_scatter<8>(v, lane);
+        const double tot = df_value(v[0]);
+        if (myv < 3) add_moment_lane<GEOM>(d, stage_sum(S0, b, comp_of(myv), tot), comp_of(myv), 2, bi, lane & 3, acc);
+        else if (myv < 6)
+            add_moment_lane<GEOM>(d, stage_sum(S0, b, comp_of(myv - 3), tot), comp_of(myv - 3), 1, bi, lane & 3, acc);
     }
-    if (!group_reduce<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
+    if (!group_reduce_split<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
     stage_done(ctl);
     if (threadIdx.x < kNJ) {
         ctl->JA1[threadIdx.x] = 0.;
@@ -393,9 +469,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
@@ -414,11 +488,11 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const KC k = warp_small_t(norm2(h) * (l1 * l1)) ? kcoef<2>(h, l1) : kcoef<5>(h, l1);
             acc_drho(x, k_apply(k, h, x), fvp[e], s0, s2, s3);
         }
-        double v[4] = {.5 * s0.value(), s2.value(), s3.value(), 0.};
-        warp_reduce_scatter<4>(v, lane);
-        if (myv < 3) add_moment<GEOM>(d, stage_sum(S0, b, comp_of(myv), v[0]), comp_of(myv), 2, bi, acc);
+        DF v[4] = {DF{.5f * s0.s, -.5f * s0.c}, DF{s2.s, -s2.c}, DF{s3.s, -s3.c}, DF{0.f, 0.f}};
+        df_reduce_scatter<4>(v, lane);
+        if (myv < 3) add_moment_lane<GEOM>(d, stage_sum(S0, b, comp_of(myv), df_value(v[0])), comp_of(myv), 2, bi, lane & 7, acc);
     }
-    if (!group_reduce<K>(rt, 8, 3, acc, 0., false, s_warp, s_out)) return;
+    if (!group_reduce_split<K>(rt, 8, 3, acc, 0., false, s_warp, s_out)) return;
     if (threadIdx.x < kNJ) ctl->JB4[threadIdx.x] = 0.;
     __syncthreads();
     if ((int)threadIdx.x < 3 * K) {
@@ -480,9 +554,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.;
+    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     double mx = -1.0;
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
@@ -537,21 +609,20 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             err = fmaf(.25f * ((t2.ar * t2.ar + t2.ai * t2.ai) + (t2.br * t2.br + t2.bi * t2.bi)), f, err);
             acc_drho(x, inc, f, s0, s2, s3);
         }
-        double v[4] = {(double)err, .5 * s0.value(), s2.value(), s3.value()};
-        warp_reduce_scatter<4>(v, lane);
-        double sv = v[0];
-        if (myv > 0) sv = stage_sum(S0, b, comp_of(myv - 1), v[0]);
-        if (myv == 0) mx = fmax(mx, v[0]);
-        else add_moment<GEOM>(d, sv, comp_of(myv - 1), 2, bi, acc);
+        DF v[4] = {DF{err, 0.f}, DF{.5f * s0.s, -.5f * s0.c}, DF{s2.s, -s2.c}, DF{s3.s, -s3.c}};
+        df_reduce_scatter<4>(v, lane);
+        const double tot = df_value(v[0]);
+        double sv = tot;
+        if (myv > 0) sv = stage_sum(S0, b, comp_of(myv - 1), tot);
+        if (myv == 0) mx = fmax(mx, tot);
+        else add_moment_lane<GEOM>(d, sv, comp_of(myv - 1), 2, bi, lane & 7, acc);
         if ((lane & 7) == 0) {
             if (myv == 0) S4[(size_t)b * 4 + 1] = 0.;
             else S4[(size_t)b * 4 + comp_of(myv - 1)] = sv;
         }
     }
-    double accs[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) accs[k] = __shfl_down_sync(kFull, acc[k], 8);
-    if (!group_reduce<K>(rt, 8, 3, accs, mx, true, s_warp, s_out)) return;
+    const double accs = __shfl_down_sync(kFull, acc, 8);
+    if (!group_reduce_split<K>(rt, 8, 3, accs, mx, true, s_warp, s_out)) return;
     if (threadIdx.x < kNJ) ctl->JC[threadIdx.x] = 0.;
     __syncthreads();
     if ((int)threadIdx.x < 3 * K) {
@@ -571,56 +642,6 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             ctl->m4lo = t;
         }
     }
-}
-
-// ------------------------------------------------------------------ double-float
-
-// Error-free transformations on FP32 (the compensated pairs' arithmetic):
-// TwoSum (Knuth), Fast2Sum (Dekker, |a| >= |b|) and the FMA-based TwoProduct.
-struct DF {
-    float h, l;
-};
-
-__device__ __forceinline__ DF two_sum(float a, float b)
-{
-    const float s = a + b;
-    const float bp = s - a;
-    return DF{s, (a - (s - bp)) + (b - bp)};
-}
-
-__device__ __forceinline__ DF fast_two_sum(float a, float b)
-{
-    const float s = a + b;
-    return DF{s, b - (s - a)};
-}
-
-__device__ __forceinline__ DF two_prod(float a, float b)
-{
-    const float p = a * b;
-    return DF{p, fmaf(a, b, -p)};
-}
-
-__device__ __forceinline__ DF df_add(const DF& a, const DF& b)
-{
-    const DF s = two_sum(a.h, b.h);
-    return fast_two_sum(s.h, s.l + (a.l + b.l));
-}
-
-__device__ __forceinline__ DF df_mul(const DF& a, const DF& b)
-{
-    const DF p = two_prod(a.h, b.h);
-    return fast_two_sum(p.h, fmaf(a.h, b.l, fmaf(a.l, b.h, p.l)));
-}
-
-// x0 x1 + y0 y1 for compensated pairs x = (x0 + xl0), ... (the lo*lo terms,
-// 2^-48 of the result, are dropped).
-__device__ __forceinline__ DF df_dot2(float x0, float xl0, float x1, float xl1, float y0, float yl0, float y1,
-                                      float yl1)
-{
-    const DF p = two_prod(x0, x1), q = two_prod(y0, y1);
-    const DF t = two_sum(p.h, q.h);
-    const float cross = fmaf(x0, xl1, fmaf(xl0, x1, fmaf(y0, yl1, yl0 * y1)));
-    return fast_two_sum(t.h, t.l + (p.l + q.l + cross));
 }
 
 // ------------------------------------------------------------------ esum / renormalisation
