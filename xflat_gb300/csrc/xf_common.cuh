@@ -455,6 +455,9 @@ __device__ inline bool step_control(const Dev& d, Ctl* ctl, double me)
         double* ts = ctl->S0;
         ctl->S0 = ctl->S4;
         ctl->S4 = ts;
+        float2* tf = ctl->S0f;  // null outside the mixed path
+        ctl->S0f = ctl->S4f;
+        ctl->S4f = tf;
         for (int i = 0; i < kNJ; ++i) ctl->J0[i] = ctl->JC[i];
         if (d.log && ctl->log_len < d.log_cap) {
             double* rec = d.log + 3 * ctl->log_len;
@@ -503,6 +506,17 @@ namespace detail {
 // path segments (src/Nmr.cpp:153-173, src/Phy_MA.cpp:172-227,
 // src/Phy_MAA.cpp:194-241) for angle bin `ang`.  Under device control angle 0
 // also evaluates the matter term at the three points (src/Matt.cpp:31-64).
+// Mirrors entry i of the geometry table as a double-float pair (mixed path).
+__device__ __forceinline__ void geo_store(const Dev& d, int i, double v)
+{
+    d.geo[i] = v;
+    if (d.geof) {
+        const float h = (float)v;
+        d.geof[i] = h;
+        d.geof[12 * d.A + i] = (float)(v - (double)h);
+    }
+}
+
 __device__ inline void geometry_body(const Dev& d, int ang)
 {
     Ctl* ctl = d.ctl;
@@ -535,13 +549,13 @@ __device__ inline void geometry_body(const Dev& d, int ang)
         for (int pt = 0; pt < 3; ++pt) {
             const double R = d.Rv / rp[pt];
             const double tm = 1. - sqrt(1. - (R * R));
-            d.geo[geo_idx(0, pt, ang, d.A)] = 0.;
-            d.geo[geo_idx(1, pt, ang, d.A)] = 0.;
-            d.geo[geo_idx(2, pt, ang, d.A)] = .5 * (tm * tm);
+            geo_store(d, geo_idx(0, pt, ang, d.A), 0.);
+            geo_store(d, geo_idx(1, pt, ang, d.A), 0.);
+            geo_store(d, geo_idx(2, pt, ang, d.A), .5 * (tm * tm));
         }
-        d.geo[geo_idx(3, 0, ang, d.A)] = dr2;
-        d.geo[geo_idx(3, 1, ang, d.A)] = dr;
-        d.geo[geo_idx(3, 2, ang, d.A)] = dr2;
+        geo_store(d, geo_idx(3, 0, ang, d.A), dr2);
+        geo_store(d, geo_idx(3, 1, ang, d.A), dr);
+        geo_store(d, geo_idx(3, 2, ang, d.A), dr2);
         return;
     }
     double c[3];
@@ -550,18 +564,18 @@ __device__ inline void geometry_body(const Dev& d, int ang)
         const double ra = d.Rv / rp[pt];
         const double r2 = ra * ra;
         c[pt] = sqrt(1. - r2 * (1. - d.cos2R[ang]));
-        d.geo[geo_idx(0, pt, ang, d.A)] = c[pt];
-        d.geo[geo_idx(1, pt, ang, d.A)] = ra * d.sinR[ang];
-        d.geo[geo_idx(2, pt, ang, d.A)] = .5 * (1. / c[pt]) * r2 * d.dcos2R[ang];
+        geo_store(d, geo_idx(0, pt, ang, d.A), c[pt]);
+        geo_store(d, geo_idx(1, pt, ang, d.A), ra * d.sinR[ang]);
+        geo_store(d, geo_idx(2, pt, ang, d.A), .5 * (1. / c[pt]) * r2 * d.dcos2R[ang]);
     }
     if (d.geom == 0) {
-        d.geo[geo_idx(3, 0, ang, d.A)] = dr2 / (c[0]);
-        d.geo[geo_idx(3, 1, ang, d.A)] = dr / (c[0]);
-        d.geo[geo_idx(3, 2, ang, d.A)] = dr2 / (c[1]);
+        geo_store(d, geo_idx(3, 0, ang, d.A), dr2 / (c[0]));
+        geo_store(d, geo_idx(3, 1, ang, d.A), dr / (c[0]));
+        geo_store(d, geo_idx(3, 2, ang, d.A), dr2 / (c[1]));
     } else {
-        d.geo[geo_idx(3, 0, ang, d.A)] = dr2 / ((c[0] + c[1]) * .5);
-        d.geo[geo_idx(3, 1, ang, d.A)] = dr / ((c[0] + c[2]) * .5);
-        d.geo[geo_idx(3, 2, ang, d.A)] = dr2 / ((c[1] + c[2]) * .5);
+        geo_store(d, geo_idx(3, 0, ang, d.A), dr2 / ((c[0] + c[1]) * .5));
+        geo_store(d, geo_idx(3, 1, ang, d.A), dr / ((c[0] + c[2]) * .5));
+        geo_store(d, geo_idx(3, 2, ang, d.A), dr2 / ((c[1] + c[2]) * .5));
     }
 }
 

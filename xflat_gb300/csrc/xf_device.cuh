@@ -50,6 +50,8 @@ struct Ctl {
     double* psi4;
     double* S0;
     double* S4;
+    float2* S0f;          // mixed precision: the sums S0 / S4 also as double-float (hi, lo) pairs
+    float2* S4f;
     float* m0hi;          // mixed precision: psi0 and candidate as FP32 value + FP32 compensation
     float* m0lo;
     float* m4hi;
@@ -105,6 +107,11 @@ struct Dev {
     const double* cosphi; // [P]
     const double* sinphi; // [P]
     double* geo;          // [4][3][A]
+    float* geof;          // [2][4][3][A]: the geometry table as double-float, hi block then lo block
+    const float* cosphif; // [2][P] azimuth tables as double-float (hi, then lo)
+    const float* sinphif;
+    float LEkf[8];        // kappa L/<E> per particle as double-float: hi[4], lo[4] (kappa ~ 1e-45 and
+                          // J ~ 1e50 are outside FP32's range; kappa J, the Hamiltonian scale, is not)
     double* psi1;
     double* psi3;
     double* partials;     // [grid][kPartStride]

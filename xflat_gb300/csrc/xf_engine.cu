@@ -120,6 +120,19 @@ int xf_handle::init(const xf_config& c)
     if ((rc = dalloc(this, &d_cosphi, cphi.size())) || (rc = upload(this, d_cosphi, cphi))) return rc;
     if ((rc = dalloc(this, &d_sinphi, sphi.size())) || (rc = upload(this, d_sinphi, sphi))) return rc;
     if ((rc = dalloc(this, &d_geo, 12 * (size_t)A))) return rc;
+    if ((rc = dalloc(this, &d_geof, 24 * (size_t)A))) return rc;
+    {
+        // azimuth tables as double-float pairs for the mixed-precision kernels
+        const int np = (int)cphi.size();
+        std::vector<float> pf(4 * (size_t)np);
+        for (int i = 0; i < np; ++i) {
+            pf[i] = (float)cphi[i];
+            pf[np + i] = (float)(cphi[i] - (double)pf[i]);
+            pf[2 * np + i] = (float)sphi[i];
+            pf[3 * np + i] = (float)(sphi[i] - (double)pf[2 * np + i]);
+        }
+        if ((rc = dalloc(this, &d_phif, pf.size())) || (rc = upload(this, d_phif, pf))) return rc;
+    }
     const int maxblk = std::max(xf::max_phase_blocks(nbeams, 256), 152 * 4);
     if ((rc = dalloc(this, &d_partials, (size_t)maxblk * xf::kPartStride))) return rc;
     if ((rc = dalloc(this, &d_ctl, 1))) return rc;
@@ -145,10 +158,18 @@ int xf_handle::init(const xf_config& c)
     dev.cosphi = d_cosphi;
     dev.sinphi = d_sinphi;
     dev.geo = d_geo;
+    dev.geof = cfg.precision == XF_PREC_MIXED ? d_geof : nullptr;  // the FP64 path reads only geo
+    dev.cosphif = d_phif;
+    dev.sinphif = d_phif + 2 * cphi.size();
     dev.partials = d_partials;
     dev.ctl = d_ctl;
     for (int p = 0; p < 4; ++p) dev.LE[p] = tab.LE[p];
     dev.kappa = tab.integ_coef;
+    for (int p = 0; p < 4; ++p) {
+        const double lk = tab.LE[p] * tab.integ_coef;
+        dev.LEkf[p] = (float)lk;
+        dev.LEkf[4 + p] = (float)(lk - (double)dev.LEkf[p]);
+    }
     dev.Rv = cfg.Rv;
     dev.eps0 = cfg.eps0;
     dev.ksi = cfg.ksi;
@@ -196,6 +217,8 @@ void xf_handle::release()
                       d_Sscratch, d_psi[0], d_psi[1], d_psi[2], d_psi[3], d_S[0], d_S[1], d_log};
     for (double* b : bufs)
         if (b) cudaFree(b);
+    if (d_geof) cudaFree(d_geof);
+    if (d_phif) cudaFree(d_phif);
     if (d_ctl) cudaFree(d_ctl);
     if (h_ctl) cudaFreeHost(h_ctl);
     if (h_in) cudaFreeHost(h_in);

@@ -33,6 +33,8 @@ struct xf_handle {
     double* d_cosphi = nullptr;
     double* d_sinphi = nullptr;
     double* d_geo = nullptr;
+    float* d_geof = nullptr;     // geometry table as double-float (mixed path)
+    float* d_phif = nullptr;     // [4][P]: cos(phi) hi, lo, sin(phi) hi, lo
     double* d_partials = nullptr;
     double* d_hvv = nullptr;
     double* d_Sscratch = nullptr;

@@ -106,6 +106,9 @@ __global__ void k_mix_accept(Dev d)
     double* ts = c->S0;
     c->S0 = c->S4;
     c->S4 = ts;
+    float2* tf = c->S0f;
+    c->S0f = c->S4f;
+    c->S4f = tf;
     for (int i = 0; i < kNJ; ++i) c->J0[i] = c->JC[i];
 }
 
@@ -120,6 +123,7 @@ struct Mixed {
     float* fvf_lo = nullptr;
     float* hvf = nullptr;
     double* S[2] = {nullptr, nullptr};
+    float2* Sf[2] = {nullptr, nullptr};
 };
 
 #define XM_CUDA(h, call)                                                                            \
@@ -137,6 +141,8 @@ Mixed* mixed_create(xf_handle* h)
         ok = ok && cudaMalloc(&m->hi[i], n * sizeof(float)) == cudaSuccess && cudaMemset(m->hi[i], 0, n * sizeof(float)) == cudaSuccess;
         ok = ok && cudaMalloc(&m->lo[i], n * sizeof(float)) == cudaSuccess && cudaMemset(m->lo[i], 0, n * sizeof(float)) == cudaSuccess;
         ok = ok && cudaMalloc(&m->S[i], 4 * (size_t)h->nbeams * sizeof(double)) == cudaSuccess;
+        ok = ok && cudaMalloc(&m->Sf[i], 4 * (size_t)h->nbeams * sizeof(float2)) == cudaSuccess &&
+             cudaMemset(m->Sf[i], 0, 4 * (size_t)h->nbeams * sizeof(float2)) == cudaSuccess;
     }
     std::vector<float> fvf(4 * (size_t)h->epad, 0.f), fvf_lo(4 * (size_t)h->epad, 0.f), hvf(2 * (size_t)h->epad, 0.f);
     for (int p = 0; p < 4; ++p)
@@ -169,6 +175,8 @@ Mixed* mixed_create(xf_handle* h)
     h->h_ctl->m4lo = m->lo[1];
     h->h_ctl->S0 = m->S[0];
     h->h_ctl->S4 = m->S[1];
+    h->h_ctl->S0f = m->Sf[0];
+    h->h_ctl->S4f = m->Sf[1];
     if (cudaMemcpy(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice) != cudaSuccess) {
         h->fail(XF_ECUDA, "control block upload failed");
         mixed_destroy(m);
@@ -184,6 +192,7 @@ void mixed_destroy(Mixed* m)
         if (m->hi[i]) cudaFree(m->hi[i]);
         if (m->lo[i]) cudaFree(m->lo[i]);
         if (m->S[i]) cudaFree(m->S[i]);
+        if (m->Sf[i]) cudaFree(m->Sf[i]);
     }
     if (m->fvf) cudaFree(m->fvf);
     if (m->fvf_lo) cudaFree(m->fvf_lo);

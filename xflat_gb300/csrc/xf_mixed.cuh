@@ -370,6 +370,105 @@ __device__ __forceinline__ void df_reduce_scatter(DF (&v)[NV], int lane)
 
 __device__ __forceinline__ double df_value(const DF& x) { return (double)x.h + (double)x.l; }
 
+__device__ __forceinline__ DF df_neg(const DF& a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF df_sub(const DF& a, const DF& b) { return df_add(a, df_neg(b)); }
+
+// ------------------------------------------------------------------ per-beam set-up and moments in double-float
+//
+// The per-beam work around the energy loop (the Hamiltonian offsets from the
+// stage moments, the path lengths and their differences, the weighted angular
+// moments) needs more than FP32 precision but not the FP64 pipe, which runs at
+// 1/64 of the FP32 rate on this GPU: it is done in double-float arithmetic on
+// tables the geometry kernel and the set-up provide as (hi, lo) pairs.  The
+// moments J and matter terms a phase reads are converted once per block.
+
+// Entry (q, pt, ang) of the geometry table as a double-float.
+__device__ __forceinline__ DF dfg(const Dev& d, int q, int pt, int ang)
+{
+    const int i = geo_idx(q, pt, ang, d.A);
+    return DF{d.geof[i], d.geof[12 * d.A + i]};
+}
+
+// The stage moments scaled by kappa (up to four sets of kNJ) and the three
+// matter terms, per block.  kappa J is the Hamiltonian's scale (J itself, of
+// order 1e50 in these units, and kappa, 1e-45, are outside FP32's range).
+struct SharedJ {
+    float h[4][kNJ], l[4][kNJ];
+    float hmh[3], hml[3];
+};
+
+__device__ __forceinline__ void split_store(double x, float& h, float& l)
+{
+    h = (float)x;
+    l = (float)(x - (double)h);
+}
+
+__device__ inline void load_shared_j(SharedJ& sj, const Ctl* ctl, double d_kappa, const double* J0, const double* J1,
+                                     const double* J2, const double* J3)
+{
+    for (int i = threadIdx.x; i < 4 * kNJ; i += blockDim.x) {
+        const int st = i / kNJ, k = i % kNJ;
+        const double* J = st == 0 ? J0 : st == 1 ? J1 : st == 2 ? J2 : J3;
+        if (J) split_store(d_kappa * J[k], sj.h[st][k], sj.l[st][k]);
+    }
+    if (threadIdx.x < 3) split_store(ctl->hm[threadIdx.x], sj.hmh[threadIdx.x], sj.hml[threadIdx.x]);
+    __syncthreads();
+}
+
+__device__ __forceinline__ DF sj_get(const SharedJ& sj, int st, int i) { return DF{sj.h[st][i], sj.l[st][i]}; }
+
+// Component k of the beam Hamiltonian offsets (beam_offset_k) at stage point
+// pt from the kappa-scaled moments of shared stage st, in double-float:
+// kJ0 - c kJ1 (MA) or kJ0 - (s cos(phi) kJx + s sin(phi) kJy + c kJz) (MAA),
+// plus the matter term on component 0, with the particle sign.
+template <int GEOM>
+__device__ __forceinline__ DF beam_offset_df(const Dev& d, const SharedJ& sj, int st, int pt, const BeamIdx& bi, int k)
+{
+    const int z = k == 0 ? 0 : (k == 1 ? 2 : 3);
+    const DF c = dfg(d, 0, pt, bi.ang);
+    DF u;
+    if (GEOM == 0) {
+        u = df_sub(sj_get(sj, st, z), df_mul(sj_get(sj, st, 4 + z), c));
+    } else {
+        const DF s = dfg(d, 1, pt, bi.ang);
+        const DF cp{d.cosphif[bi.phi], d.cosphif[d.P + bi.phi]}, sp{d.sinphif[bi.phi], d.sinphif[d.P + bi.phi]};
+        const DF t = df_add(df_add(df_mul(df_mul(s, cp), sj_get(sj, st, 4 + z)), df_mul(df_mul(s, sp), sj_get(sj, st, 8 + z))),
+                            df_mul(c, sj_get(sj, st, 12 + z)));
+        u = df_sub(sj_get(sj, st, z), t);
+    }
+    DF H = u;
+    if (k == 0) H = df_add(H, DF{sj.hmh[pt], sj.hml[pt]});
+    return (k < 2 && (bi.p & 1)) ? df_neg(H) : H;
+}
+
+// add_moment_lane in double-float, scaled by kappa (the weight kappa L/<E>):
+// lane k of a value group accumulates kappa times moment k; the block totals
+// are divided by kappa in FP64 when the moments are written.
+template <int GEOM>
+__device__ __forceinline__ void add_moment_df(const Dev& d, const DF& val, int z, int pt, const BeamIdx& bi, int k, DF& acc)
+{
+    if (k >= NK<GEOM>::K) return;
+    DF c = df_mul(val, DF{d.LEkf[bi.p], d.LEkf[4 + bi.p]});
+    if (!(z == 3 || (bi.p & 1) == 0)) c = df_neg(c);
+    const DF dc = dfg(d, 2, pt, bi.ang);
+    DF m;
+    if (GEOM == 0 || k == 0 || k == 3) {
+        m = df_mul(c, dc);
+        if (k != 0) m = df_mul(m, dfg(d, 0, pt, bi.ang));
+    } else {
+        const DF a = k == 1 ? DF{d.cosphif[bi.phi], d.cosphif[d.P + bi.phi]} : DF{d.sinphif[bi.phi], d.sinphif[d.P + bi.phi]};
+        m = df_mul(df_mul(df_mul(c, a), dfg(d, 1, pt, bi.ang)), dc);
+    }
+    acc = df_add(acc, m);
+}
+
+// psi0's sum of density component comp for beam b, as a double-float.
+__device__ __forceinline__ DF s0_df(const Ctl* ctl, int b, int comp)
+{
+    const float2 v = ctl->S0f[(size_t)b * 4 + comp];
+    return DF{v.x, v.y};
+}
+
 // ------------------------------------------------------------------ phase A
 
 // Moments of psi1 = U(h0, dl1) psi0 at point 2 and of psi3 = U(h0, dl0) psi0 at point 1.
@@ -381,12 +480,13 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     if (ctl->done) return;
     __shared__ double s_warp[8 * 32];
     __shared__ double s_out[32];
+    __shared__ SharedJ sj;
+    if (GEOM == 1) load_shared_j(sj, ctl, d.kappa, ctl->J0, nullptr, nullptr, nullptr);
     const float* __restrict__ p0 = ctl->m0hi;
-    const double* __restrict__ S0 = ctl->S0;
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
+    DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
     const int myv = lane >> 2;
     const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
     for (int b = gw; b < d.nbeams; b += tw) {
@@ -394,8 +494,10 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         if (stage) stage_beam(d, ctl, stage, b, lane, nullptr, ctl->m0hi, ctl->m0lo);
         // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
         float sv = 0.f;
-        if (lane < 3) sv = (float)beam_offset_k<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi, lane);
-        else if (lane < 5) sv = (float)geo(d, 3, lane - 3, bi.ang);
+        if (lane < 3)
+            sv = GEOM == 0 ? (float)beam_offset_k<GEOM>(d, ctl->J0, 0, ctl->hm[0], bi, lane)
+                           : beam_offset_df<GEOM>(d, sj, 0, 0, bi, lane).h;
+        else if (lane < 5) sv = d.geof[geo_idx(3, lane - 3, bi.ang, d.A)];
         const H3f g0 = shfl_h3(sv, 0);
         const float l0 = __shfl_sync(kFull, sv, 3), l1 = __shfl_sync(kFull, sv, 4);
         const float* in = p0 + (size_t)b * 4 * epad;
@@ -434,12 +536,11 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         v[0] = DF{.5f * v[0].h, .5f * v[0].l};
         v[3] = DF{.5f * v[3].h, .5f * v[3].l};
         df_reduce_scatter<8>(v, lane);
-        const double tot = df_value(v[0]);
-        if (myv < 3) add_moment_lane<GEOM>(d, stage_sum(S0, b, comp_of(myv), tot), comp_of(myv), 2, bi, lane & 3, acc);
+        if (myv < 3) add_moment_df<GEOM>(d, df_add(s0_df(ctl, b, comp_of(myv)), v[0]), comp_of(myv), 2, bi, lane & 3, acc);
         else if (myv < 6)
-            add_moment_lane<GEOM>(d, stage_sum(S0, b, comp_of(myv - 3), tot), comp_of(myv - 3), 1, bi, lane & 3, acc);
+            add_moment_df<GEOM>(d, df_add(s0_df(ctl, b, comp_of(myv - 3)), v[0]), comp_of(myv - 3), 1, bi, lane & 3, acc);
     }
-    if (!group_reduce_split<K>(rt, 4, 6, acc, 0., false, s_warp, s_out)) return;
+    if (!group_reduce_split<K>(rt, 4, 6, df_value(acc), 0., false, s_warp, s_out)) return;
     stage_done(ctl);
     if (threadIdx.x < kNJ) {
         ctl->JA1[threadIdx.x] = 0.;
@@ -449,7 +550,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     if ((int)threadIdx.x < 6 * K) {
         const int v = threadIdx.x / K, k = threadIdx.x % K;
         double* J = v < 3 ? ctl->JA1 : ctl->JA3;
-        J[k * 4 + comp_of(v % 3)] = s_out[threadIdx.x];
+        J[k * 4 + comp_of(v % 3)] = s_out[threadIdx.x] / d.kappa;
     }
 }
 
@@ -464,19 +565,22 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     if (ctl->done) return;
     __shared__ double s_warp[8 * 32];
     __shared__ double s_out[32];
+    __shared__ SharedJ sj;
+    if (GEOM == 1) load_shared_j(sj, ctl, d.kappa, ctl->JA3, nullptr, nullptr, nullptr);
     const float* __restrict__ p0 = ctl->m0hi;
-    const double* __restrict__ S0 = ctl->S0;
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
+    DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up: lanes 0-2 the offsets of H3, lane 3 dl1
         float sv = 0.f;
-        if (lane < 3) sv = (float)beam_offset_k<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi, lane);
-        else if (lane == 3) sv = (float)geo(d, 3, 1, bi.ang);
+        if (lane < 3)
+            sv = GEOM == 0 ? (float)beam_offset_k<GEOM>(d, ctl->JA3, 1, ctl->hm[1], bi, lane)
+                           : beam_offset_df<GEOM>(d, sj, 0, 1, bi, lane).h;
+        else if (lane == 3) sv = d.geof[geo_idx(3, 1, bi.ang, d.A)];
         const H3f g3 = shfl_h3(sv, 0);
         const float l1 = __shfl_sync(kFull, sv, 3);
         const float* in = p0 + (size_t)b * 4 * epad;
@@ -490,14 +594,14 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         }
         DF v[4] = {DF{.5f * s0.s, -.5f * s0.c}, DF{s2.s, -s2.c}, DF{s3.s, -s3.c}, DF{0.f, 0.f}};
         df_reduce_scatter<4>(v, lane);
-        if (myv < 3) add_moment_lane<GEOM>(d, stage_sum(S0, b, comp_of(myv), df_value(v[0])), comp_of(myv), 2, bi, lane & 7, acc);
+        if (myv < 3) add_moment_df<GEOM>(d, df_add(s0_df(ctl, b, comp_of(myv)), v[0]), comp_of(myv), 2, bi, lane & 7, acc);
     }
-    if (!group_reduce_split<K>(rt, 8, 3, acc, 0., false, s_warp, s_out)) return;
+    if (!group_reduce_split<K>(rt, 8, 3, df_value(acc), 0., false, s_warp, s_out)) return;
     if (threadIdx.x < kNJ) ctl->JB4[threadIdx.x] = 0.;
     __syncthreads();
     if ((int)threadIdx.x < 3 * K) {
         const int v = threadIdx.x / K, k = threadIdx.x % K;
-        ctl->JB4[k * 4 + comp_of(v)] = s_out[threadIdx.x];
+        ctl->JB4[k * 4 + comp_of(v)] = s_out[threadIdx.x] / d.kappa;
     }
 }
 
@@ -545,17 +649,19 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     if (ctl->done) return;
     __shared__ double s_warp[8 * 32];
     __shared__ double s_out[32];
+    __shared__ SharedJ sj;
+    if (GEOM == 1) load_shared_j(sj, ctl, d.kappa, ctl->J0, ctl->JA1, ctl->JA3, ctl->JB4);
     const float* __restrict__ hi0 = ctl->m0hi;
     const float* __restrict__ lo0 = ctl->m0lo;
     float* __restrict__ hi4 = ctl->m4hi;
     float* __restrict__ lo4 = ctl->m4lo;
-    const double* __restrict__ S0 = ctl->S0;
     double* __restrict__ S4 = ctl->S4;
+    float2* __restrict__ S4f = ctl->S4f;
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
     const int epad = d.epad;
-    double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
-    double mx = -1.0;
+    DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
+    float mx = -1.f;
     const int myv = lane >> 3;
     for (int b = gw; b < d.nbeams; b += tw) {
         const BeamIdx bi = decode_beam(d, b);
@@ -564,17 +670,25 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         // dl0, dl1, dl2, dl2 - dl0 and 2 dl0 - dl1 (18-22)
         float su = 0.f;  // this lane's scalar
         if (lane < 18) {
+            // stage s: 0 the start (J0, point 0), 1 A1 (point 2), 2 A3 (point 1), 3 B4 (point 2)
             const int k = lane % 3;
             const int sa = lane < 12 ? lane / 3 : (lane < 15 ? 2 : 3);
             const int sb = lane < 12 ? sa : (lane < 15 ? 1 : 0);
-            const double va = stage_offset<GEOM>(d, ctl, sa, bi, k);
-            const double vb = stage_offset<GEOM>(d, ctl, sb, bi, k);
-            su = (float)(lane < 12 ? va : va - vb);
+            if (GEOM == 0) {
+                // MA: two FP64 operations per offset, cheaper than the double-float route
+                const double va = stage_offset<GEOM>(d, ctl, sa, bi, k);
+                const double vb = stage_offset<GEOM>(d, ctl, sb, bi, k);
+                su = (float)(lane < 12 ? va : va - vb);
+            } else {
+                const DF va = beam_offset_df<GEOM>(d, sj, sa, sa == 0 ? 0 : sa == 2 ? 1 : 2, bi, k);
+                const DF vb = beam_offset_df<GEOM>(d, sj, sb, sb == 0 ? 0 : sb == 2 ? 1 : 2, bi, k);
+                su = lane < 12 ? va.h : df_sub(va, vb).h;
+            }
         } else if (lane < 23) {
-            const double L0 = geo(d, 3, 0, bi.ang), L1 = geo(d, 3, 1, bi.ang), L2 = geo(d, 3, 2, bi.ang);
+            const DF L0 = dfg(d, 3, 0, bi.ang), L1 = dfg(d, 3, 1, bi.ang), L2 = dfg(d, 3, 2, bi.ang);
             const int j = lane - 18;
             // the last, 2 dl0 - dl1, is zero in MA
-            su = (float)(j == 0 ? L0 : j == 1 ? L1 : j == 2 ? L2 : j == 3 ? L2 - L0 : 2.0 * L0 - L1);
+            su = j == 0 ? L0.h : j == 1 ? L1.h : j == 2 ? L2.h : j == 3 ? df_sub(L2, L0).h : df_sub(df_add(L0, L0), L1).h;
         }
         const H3f g0 = shfl_h3(su, 0), g1 = shfl_h3(su, 3), g3 = shfl_h3(su, 6), g4 = shfl_h3(su, 9);
         const H3f d31 = shfl_h3(su, 12), d40 = shfl_h3(su, 15);
@@ -611,23 +725,29 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         }
         DF v[4] = {DF{err, 0.f}, DF{.5f * s0.s, -.5f * s0.c}, DF{s2.s, -s2.c}, DF{s3.s, -s3.c}};
         df_reduce_scatter<4>(v, lane);
-        const double tot = df_value(v[0]);
-        double sv = tot;
-        if (myv > 0) sv = stage_sum(S0, b, comp_of(myv - 1), tot);
-        if (myv == 0) mx = fmax(mx, tot);
-        else add_moment_lane<GEOM>(d, sv, comp_of(myv - 1), 2, bi, lane & 7, acc);
-        if ((lane & 7) == 0) {
-            if (myv == 0) S4[(size_t)b * 4 + 1] = 0.;
-            else S4[(size_t)b * 4 + comp_of(myv - 1)] = sv;
+        if (myv == 0) {
+            mx = fmaxf(mx, v[0].h + v[0].l);
+            if ((lane & 7) == 0) {
+                S4[(size_t)b * 4 + 1] = 0.;
+                S4f[(size_t)b * 4 + 1] = make_float2(0.f, 0.f);
+            }
+        } else {
+            const int comp = comp_of(myv - 1);
+            const DF sv = df_add(s0_df(ctl, b, comp), v[0]);
+            add_moment_df<GEOM>(d, sv, comp, 2, bi, lane & 7, acc);
+            if ((lane & 7) == 0) {
+                S4[(size_t)b * 4 + comp] = df_value(sv);
+                S4f[(size_t)b * 4 + comp] = make_float2(sv.h, sv.l);
+            }
         }
     }
-    const double accs = __shfl_down_sync(kFull, acc, 8);
-    if (!group_reduce_split<K>(rt, 8, 3, accs, mx, true, s_warp, s_out)) return;
+    const double accs = __shfl_down_sync(kFull, df_value(acc), 8);
+    if (!group_reduce_split<K>(rt, 8, 3, accs, (double)mx, true, s_warp, s_out)) return;
     if (threadIdx.x < kNJ) ctl->JC[threadIdx.x] = 0.;
     __syncthreads();
     if ((int)threadIdx.x < 3 * K) {
         const int v = threadIdx.x / K, k = threadIdx.x % K;
-        ctl->JC[k * 4 + comp_of(v)] = s_out[threadIdx.x];
+        ctl->JC[k * 4 + comp_of(v)] = s_out[threadIdx.x] / d.kappa;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -760,7 +880,13 @@ __device__ inline void esum_body(const Dev& d, int first, int stride, int renorm
         v[1] *= .5;
         warp_reduce_scatter<4>(v, lane);
         const int myv = lane >> 3;
-        if ((lane & 7) == 0) S[(size_t)b * 4 + (myv == 0 ? 1 : comp_of(myv - 1))] = (myv == 0) ? 0. : v[0];
+        if ((lane & 7) == 0) {
+            const size_t i = (size_t)b * 4 + (myv == 0 ? 1 : comp_of(myv - 1));
+            const double x = (myv == 0) ? 0. : v[0];
+            S[i] = x;
+            const float xh = (float)x;
+            ctl->S0f[i] = make_float2(xh, (float)(x - (double)xh));
+        }
     }
 }
 }  // namespace mixed
