@@ -12,26 +12,29 @@ using namespace detail;
 
 constexpr double kSeriesT = 0.25;
 
-// cos(sqrt(t)) and sin(sqrt(t))/sqrt(t) for 0 <= t <= kSeriesT, degree 7 in t.
-// Truncation error below 7.3e-19 (cos) and 4.3e-20 (sinc) at t = 0.25.
+// cos(sqrt(t)) and sin(sqrt(t))/sqrt(t) for 0 <= t <= kSeriesT, degree 7 in t
+// (times Q, 1 or 1/2: see su2_coeffs).  Truncation error below 7.3e-19 (cos)
+// and 4.3e-20 (sinc) at t = 0.25.
+template <int Q2>
 __device__ __forceinline__ void series_cs(double t, double& c, double& s)
 {
-    c = -1.0 / 87178291200.0;
-    c = fma(c, t, 1.0 / 479001600.0);
-    c = fma(c, t, -1.0 / 3628800.0);
-    c = fma(c, t, 1.0 / 40320.0);
-    c = fma(c, t, -1.0 / 720.0);
-    c = fma(c, t, 1.0 / 24.0);
-    c = fma(c, t, -0.5);
-    c = fma(c, t, 1.0);
-    s = -1.0 / 1307674368000.0;
-    s = fma(s, t, 1.0 / 6227020800.0);
-    s = fma(s, t, -1.0 / 39916800.0);
-    s = fma(s, t, 1.0 / 362880.0);
-    s = fma(s, t, -1.0 / 5040.0);
-    s = fma(s, t, 1.0 / 120.0);
-    s = fma(s, t, -1.0 / 6.0);
-    s = fma(s, t, 1.0);
+    constexpr double q = Q2 ? 0.5 : 1.0;
+    c = q * (-1.0 / 87178291200.0);
+    c = fma(c, t, q * (1.0 / 479001600.0));
+    c = fma(c, t, q * (-1.0 / 3628800.0));
+    c = fma(c, t, q * (1.0 / 40320.0));
+    c = fma(c, t, q * (-1.0 / 720.0));
+    c = fma(c, t, q * (1.0 / 24.0));
+    c = fma(c, t, q * -0.5);
+    c = fma(c, t, q);
+    s = q * (-1.0 / 1307674368000.0);
+    s = fma(s, t, q * (1.0 / 6227020800.0));
+    s = fma(s, t, q * (-1.0 / 39916800.0));
+    s = fma(s, t, q * (1.0 / 362880.0));
+    s = fma(s, t, q * (-1.0 / 5040.0));
+    s = fma(s, t, q * (1.0 / 120.0));
+    s = fma(s, t, q * (-1.0 / 6.0));
+    s = fma(s, t, q);
 }
 
 // Coefficients (C, S) of U = C - i S H for H = [[h00, h01],[h01*, -h00]],
@@ -44,34 +47,42 @@ __device__ __forceinline__ void series_cs(double t, double& c, double& s)
 // t^4/8! <= 2.5e-17 for t <= 1e-3, t^5/10! <= 2.8e-17 for t <= 1e-2).  The
 // thresholds are compared as bit patterns (t >= 0), on the integer pipe.
 // Must be called by all 32 lanes of the warp.
+//
+// With Q2 set the coefficients come out halved, exactly (every constant of the
+// series is halved, and binary scaling commutes with rounding): U/2 psi then
+// costs nothing extra, and the averaging stages (S4/S5, S10/S11), which form
+// (U psi + psi')/2, become a plain sum of halves with the same bits as before.
 constexpr long long kT2 = 0x3EF4F8B588E368F1LL;  // 2e-5
 constexpr long long kT3 = 0x3F50624DD2F1A9FCLL;  // 1e-3
 constexpr long long kT4 = 0x3F847AE147AE147BLL;  // 1e-2
 
+template <int Q2 = 0>
 __device__ __forceinline__ void su2_coeffs(double h00, double h01r, double h01i, double dl, double& C, double& S)
 {
+    constexpr double q = Q2 ? 0.5 : 1.0;
     const double lam2 = h00 * h00 + (h01r * h01r + h01i * h01i);
     const double t = lam2 * (dl * dl);
     const long long tb = __double_as_longlong(t);
     if (__all_sync(kFull, tb <= kT2)) {
-        C = fma(fma(t, 1.0 / 24.0, -0.5), t, 1.0);
-        S = fma(fma(t, 1.0 / 120.0, -1.0 / 6.0), t, 1.0) * dl;
+        C = fma(fma(t, q * (1.0 / 24.0), q * -0.5), t, q);
+        S = fma(fma(t, q * (1.0 / 120.0), q * (-1.0 / 6.0)), t, q) * dl;
     } else if (__all_sync(kFull, tb <= kT3)) {
-        C = fma(fma(fma(t, -1.0 / 720.0, 1.0 / 24.0), t, -0.5), t, 1.0);
-        S = fma(fma(fma(t, -1.0 / 5040.0, 1.0 / 120.0), t, -1.0 / 6.0), t, 1.0) * dl;
+        C = fma(fma(fma(t, q * (-1.0 / 720.0), q * (1.0 / 24.0)), t, q * -0.5), t, q);
+        S = fma(fma(fma(t, q * (-1.0 / 5040.0), q * (1.0 / 120.0)), t, q * (-1.0 / 6.0)), t, q) * dl;
     } else if (__all_sync(kFull, tb <= kT4)) {
-        C = fma(fma(fma(fma(t, 1.0 / 40320.0, -1.0 / 720.0), t, 1.0 / 24.0), t, -0.5), t, 1.0);
-        S = fma(fma(fma(fma(t, 1.0 / 362880.0, -1.0 / 5040.0), t, 1.0 / 120.0), t, -1.0 / 6.0), t, 1.0) * dl;
+        C = fma(fma(fma(fma(t, q * (1.0 / 40320.0), q * (-1.0 / 720.0)), t, q * (1.0 / 24.0)), t, q * -0.5), t, q);
+        S = fma(fma(fma(fma(t, q * (1.0 / 362880.0), q * (-1.0 / 5040.0)), t, q * (1.0 / 120.0)), t, q * (-1.0 / 6.0)),
+                t, q) * dl;
     } else if (t <= kSeriesT) {
         double s;
-        series_cs(t, C, s);
+        series_cs<Q2>(t, C, s);
         S = s * dl;
     } else {
         const double lam = sqrt(lam2);
         double sn, cs;
         sincos(lam * dl, &sn, &cs);
-        C = cs;
-        S = sn / lam;
+        C = cs * q;
+        S = (sn / lam) * q;
     }
 }
 
@@ -166,10 +177,12 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
                 // MA: dl0 = dl1/2 exactly, so U(dl1) coefficients follow from
                 // the half-length ones by the double-angle identities.
                 su2_coeffs(h00, h01r, h.h01i, dl0, C0, S0);
-                C1 = fma(C0 + C0, C0, -1.0);
-                S1 = (C0 + C0) * S0;
+                // the halved U(dl1) (psi1 is stored halved, see su2_coeffs):
+                // C1/2 = C0^2 - 1/2 and S1/2 = C0 S0, exactly half of 2C0^2 - 1 and 2 C0 S0
+                C1 = fma(C0, C0, -0.5);
+                S1 = C0 * S0;
             } else {
-                su2_coeffs(h00, h01r, h.h01i, dl1, C1, S1);
+                su2_coeffs<1>(h00, h01r, h.h01i, dl1, C1, S1);
                 su2_coeffs(h00, h01r, h.h01i, dl0, C0, S0);
             }
             const Psi y1 = su2_apply(C1, S1, h00, h01r, h.h01i, x);
@@ -180,7 +193,10 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
             acc_rho(y1, f, v[0], v[1], v[2]);
             acc_rho(y3, f, v[3], v[4], v[5]);
         }
-        v[0] *= .5;
+        // psi1 was accumulated halved: its sums are a quarter (exactly) of psi1's
+        v[0] *= 2.;
+        v[1] *= 4.;
+        v[2] *= 4.;
         v[3] *= .5;
         warp_reduce_scatter<8>(v, lane);
         if (myv < 3) add_moment_lane<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 3, acc);
@@ -239,22 +255,27 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const Psi x = load_psi(in, epad, e);
             double C, S;
             const double a00 = hv0 + g1.h00b, a01 = hv1 + g1.h01rb;
-            su2_coeffs(a00, a01, g1.h01i, dl1, C, S);
+            // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
+            su2_coeffs<1>(a00, a01, g1.h01i, dl1, C, S);
             const Psi ya = su2_apply(C, S, a00, a01, g1.h01i, x);
             const Psi p1 = load_psi(io1, epad, e);
             Psi avg;
-            avg.ar = (ya.ar + p1.ar) * .5;
-            avg.ai = (ya.ai + p1.ai) * .5;
-            avg.br = (ya.br + p1.br) * .5;
-            avg.bi = (ya.bi + p1.bi) * .5;
+            avg.ar = ya.ar + p1.ar;
+            avg.ai = ya.ai + p1.ai;
+            avg.br = ya.br + p1.br;
+            avg.bi = ya.bi + p1.bi;
             store_psi(io1, epad, e, avg);
             const double b00 = hv0 + g3.h00b, b01 = hv1 + g3.h01rb;
-            su2_coeffs(b00, b01, g3.h01i, dl1, C, S);
+            // S8, stored halved for the average of S10/S11
+            su2_coeffs<1>(b00, b01, g3.h01i, dl1, C, S);
             const Psi y4 = su2_apply(C, S, b00, b01, g3.h01i, x);
             store_psi(o4, epad, e, y4);
             acc_rho(y4, fvp[e], v[0], v[1], v[2]);
         }
-        v[0] *= .5;
+        // psi4 was accumulated halved: its sums are a quarter (exactly) of psi4's
+        v[0] *= 2.;
+        v[1] *= 4.;
+        v[2] *= 4.;
         warp_reduce_scatter<4>(v, lane);
         if (myv < 3) add_moment_lane<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 7, acc);
     }
@@ -308,15 +329,23 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             const double a00 = d.hvac[e] + g.h00b, a01 = d.hvac[epad + e] + g.h01rb;
             const Psi x3 = load_psi(io3, epad, e);
             double C, S;
-            su2_coeffs(a00, a01, g.h01i, dl2, C, S);
+            // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
+            su2_coeffs<1>(a00, a01, g.h01i, dl2, C, S);
             const Psi y3 = su2_apply(C, S, a00, a01, g.h01i, x3);
-            if (d.debug_psi3) store_psi(io3, epad, e, y3);
+            if (d.debug_psi3) {
+                Psi full;
+                full.ar = 2. * y3.ar;
+                full.ai = 2. * y3.ai;
+                full.br = 2. * y3.br;
+                full.bi = 2. * y3.bi;
+                store_psi(io3, epad, e, full);
+            }
             const Psi x4 = load_psi(io4, epad, e);
             Psi c;
-            c.ar = (y3.ar + x4.ar) * .5;
-            c.ai = (y3.ai + x4.ai) * .5;
-            c.br = (y3.br + x4.br) * .5;
-            c.bi = (y3.bi + x4.bi) * .5;
+            c.ar = y3.ar + x4.ar;
+            c.ai = y3.ai + x4.ai;
+            c.br = y3.br + x4.br;
+            c.bi = y3.bi + x4.bi;
             store_psi(io4, epad, e, c);
             const Psi r1 = load_psi(p1b, epad, e);
             const double f = fvp[e];
