@@ -105,8 +105,9 @@ __device__ __forceinline__ Psi su2_apply(double C, double S, double h00, double 
 }
 
 // The same propagator written U psi = C psi + S w with w = -i sigma(h) psi:
-// w costs 12 operations once per Hamiltonian and each U psi then 8, so two
-// propagators sharing h (phase A's two path lengths) cost 28 instead of 38.
+// w costs 12 FP64 operations (4 products fused into 8 FMAs) and U psi then 8,
+// against 23 for su2_apply's grouping, and two propagators sharing h (phase
+// A's two path lengths) share w.  Used for every propagator of the FP64 path.
 __device__ __forceinline__ Psi su2_w(double h00, double h01r, double h01i, const Psi& x)
 {
     Psi w;
@@ -281,7 +282,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const double a00 = hv0 + g1.h00b, a01 = hv1 + g1.h01rb;
             // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
             su2_coeffs<1>(a00, a01, g1.h01i, dl1, C, S);
-            const Psi ya = su2_apply(C, S, a00, a01, g1.h01i, x);
+            const Psi ya = su2_apply_w(C, S, x, su2_w(a00, a01, g1.h01i, x));
             const Psi p1 = load_psi(io1, epad, e);
             Psi avg;
             avg.ar = ya.ar + p1.ar;
@@ -292,7 +293,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const double b00 = hv0 + g3.h00b, b01 = hv1 + g3.h01rb;
             // S8, stored halved for the average of S10/S11
             su2_coeffs<1>(b00, b01, g3.h01i, dl1, C, S);
-            const Psi y4 = su2_apply(C, S, b00, b01, g3.h01i, x);
+            const Psi y4 = su2_apply_w(C, S, x, su2_w(b00, b01, g3.h01i, x));
             store_psi(o4, epad, e, y4);
             acc_rho(y4, fvp[e], v[0], v[1], v[2]);
         }
@@ -355,7 +356,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             double C, S;
             // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
             su2_coeffs<1>(a00, a01, g.h01i, dl2, C, S);
-            const Psi y3 = su2_apply(C, S, a00, a01, g.h01i, x3);
+            const Psi y3 = su2_apply_w(C, S, x3, su2_w(a00, a01, g.h01i, x3));
             if (d.debug_psi3) {
                 Psi full;
                 full.ar = 2. * y3.ar;
