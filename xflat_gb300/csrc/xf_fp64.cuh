@@ -86,28 +86,16 @@ __device__ __forceinline__ void su2_coeffs(double h00, double h01r, double h01i,
     }
 }
 
-// psi' = U psi with the matrix entries of src/NBeam.cpp:371-392.
+// A bin of a beam state: psi = (a, b) = (ar + i ai, br + i bi).
 struct Psi {
     double ar, ai, br, bi;
 };
 
-__device__ __forceinline__ Psi su2_apply(double C, double S, double h00, double h01r, double h01i, const Psi& x)
-{
-    const double m1 = -h00 * S;
-    const double m2 = h01i * S;
-    const double m3 = -h01r * S;
-    Psi y;
-    y.ar = (C * x.ar - m1 * x.ai) + (m2 * x.br - m3 * x.bi);
-    y.ai = (C * x.ai + m1 * x.ar) + (m2 * x.bi + m3 * x.br);
-    y.br = (-m2 * x.ar - m3 * x.ai) + (C * x.br + m1 * x.bi);
-    y.bi = (-m2 * x.ai + m3 * x.ar) + (C * x.bi - m1 * x.br);
-    return y;
-}
-
-// The same propagator written U psi = C psi + S w with w = -i sigma(h) psi:
-// w costs 12 FP64 operations (4 products fused into 8 FMAs) and U psi then 8,
-// against 23 for su2_apply's grouping, and two propagators sharing h (phase
-// A's two path lengths) share w.  Used for every propagator of the FP64 path.
+// psi' = U psi with the matrix entries of src/NBeam.cpp:371-392, written
+// U psi = C psi + S w with w = -i sigma(h) psi: w costs 12 FP64 operations
+// (products fused into FMAs) and U psi then 8, against 23 for the entries
+// grouped as in the reference, and two propagators sharing h (phase A's two
+// path lengths) share w.
 __device__ __forceinline__ Psi su2_w(double h00, double h01r, double h01i, const Psi& x)
 {
     Psi w;
