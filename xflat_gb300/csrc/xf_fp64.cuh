@@ -56,16 +56,39 @@ constexpr long long kT2 = 0x3EF4F8B588E368F1LL;  // 2e-5
 constexpr long long kT3 = 0x3F50624DD2F1A9FCLL;  // 1e-3
 constexpr long long kT4 = 0x3F847AE147AE147BLL;  // 1e-2
 
+// Per-beam constants of one propagator: h01i (not energy dependent) squared,
+// dl^2, and the degree-2 sinc polynomial's coefficients times dl, so that the
+// common branch of su2_coeffs costs 2 + 1 + 2 + 2 FP64 operations per bin.
+struct PropK {
+    double dl, dl2, h01i2;
+    double s0, s1, s2;  // q dl (1, -1/6, 1/120)
+};
+
 template <int Q2 = 0>
-__device__ __forceinline__ void su2_coeffs(double h00, double h01r, double h01i, double dl, double& C, double& S)
+__device__ __forceinline__ PropK prop_k(double h01i, double dl)
 {
     constexpr double q = Q2 ? 0.5 : 1.0;
-    const double lam2 = h00 * h00 + (h01r * h01r + h01i * h01i);
-    const double t = lam2 * (dl * dl);
+    PropK p;
+    p.dl = dl;
+    p.dl2 = dl * dl;
+    p.h01i2 = h01i * h01i;
+    p.s0 = q * dl;
+    p.s1 = (q * (-1.0 / 6.0)) * dl;
+    p.s2 = (q * (1.0 / 120.0)) * dl;
+    return p;
+}
+
+template <int Q2 = 0>
+__device__ __forceinline__ void su2_coeffs(double h00, double h01r, const PropK& pk, double& C, double& S)
+{
+    constexpr double q = Q2 ? 0.5 : 1.0;
+    const double dl = pk.dl;
+    const double lam2 = fma(h00, h00, fma(h01r, h01r, pk.h01i2));
+    const double t = lam2 * pk.dl2;
     const long long tb = __double_as_longlong(t);
     if (__all_sync(kFull, tb <= kT2)) {
         C = fma(fma(t, q * (1.0 / 24.0), q * -0.5), t, q);
-        S = fma(fma(t, q * (1.0 / 120.0), q * (-1.0 / 6.0)), t, q) * dl;
+        S = fma(fma(t, pk.s2, pk.s1), t, pk.s0);
     } else if (__all_sync(kFull, tb <= kT3)) {
         C = fma(fma(fma(t, q * (-1.0 / 720.0), q * (1.0 / 24.0)), t, q * -0.5), t, q);
         S = fma(fma(fma(t, q * (-1.0 / 5040.0), q * (1.0 / 120.0)), t, q * (-1.0 / 6.0)), t, q) * dl;
@@ -175,6 +198,8 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         else if (lane < 5) sv = geo(d, 3, lane - 3, bi.ang);
         const BeamH h = shfl_beamh(sv, 0);
         const double dl0 = __shfl_sync(kFull, sv, 3), dl1 = __shfl_sync(kFull, sv, 4);
+        const PropK pk0 = prop_k(h.h01i, dl0);
+        const PropK pk1 = prop_k<1>(h.h01i, dl1);  // MAA only
         const double* in = psi0 + (size_t)b * 4 * epad;
         double* o1 = d.psi1 + (size_t)b * 4 * epad;
         double* o3 = d.psi3 + (size_t)b * 4 * epad;
@@ -188,14 +213,14 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
             if (GEOM == 0) {
                 // MA: dl0 = dl1/2 exactly, so U(dl1) coefficients follow from
                 // the half-length ones by the double-angle identities.
-                su2_coeffs(h00, h01r, h.h01i, dl0, C0, S0);
+                su2_coeffs(h00, h01r, pk0, C0, S0);
                 // the halved U(dl1) (psi1 is stored halved, see su2_coeffs):
                 // C1/2 = C0^2 - 1/2 and S1/2 = C0 S0, exactly half of 2C0^2 - 1 and 2 C0 S0
                 C1 = fma(C0, C0, -0.5);
                 S1 = C0 * S0;
             } else {
-                su2_coeffs<1>(h00, h01r, h.h01i, dl1, C1, S1);
-                su2_coeffs(h00, h01r, h.h01i, dl0, C0, S0);
+                su2_coeffs<1>(h00, h01r, pk1, C1, S1);
+                su2_coeffs(h00, h01r, pk0, C0, S0);
             }
             const Psi w = su2_w(h00, h01r, h.h01i, x);
             const Psi y1 = su2_apply_w(C1, S1, x, w);
@@ -258,6 +283,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         else if (lane == 6) sv = geo(d, 3, 1, bi.ang);
         const BeamH g1 = shfl_beamh(sv, 0), g3 = shfl_beamh(sv, 3);
         const double dl1 = __shfl_sync(kFull, sv, 6);
+        const PropK pka = prop_k<1>(g1.h01i, dl1), pkb = prop_k<1>(g3.h01i, dl1);
         const double* in = psi0 + (size_t)b * 4 * epad;
         double* io1 = d.psi1 + (size_t)b * 4 * epad;
         double* o4 = psi4 + (size_t)b * 4 * epad;
@@ -269,7 +295,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             double C, S;
             const double a00 = hv0 + g1.h00b, a01 = hv1 + g1.h01rb;
             // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
-            su2_coeffs<1>(a00, a01, g1.h01i, dl1, C, S);
+            su2_coeffs<1>(a00, a01, pka, C, S);
             const Psi ya = su2_apply_w(C, S, x, su2_w(a00, a01, g1.h01i, x));
             const Psi p1 = load_psi(io1, epad, e);
             Psi avg;
@@ -280,7 +306,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             store_psi(io1, epad, e, avg);
             const double b00 = hv0 + g3.h00b, b01 = hv1 + g3.h01rb;
             // S8, stored halved for the average of S10/S11
-            su2_coeffs<1>(b00, b01, g3.h01i, dl1, C, S);
+            su2_coeffs<1>(b00, b01, pkb, C, S);
             const Psi y4 = su2_apply_w(C, S, x, su2_w(b00, b01, g3.h01i, x));
             store_psi(o4, epad, e, y4);
             acc_rho(y4, fvp[e], v[0], v[1], v[2]);
@@ -333,6 +359,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         else if (lane == 3) sv = geo(d, 3, 2, bi.ang);
         const BeamH g = shfl_beamh(sv, 0);
         const double dl2 = __shfl_sync(kFull, sv, 3);
+        const PropK pk = prop_k<1>(g.h01i, dl2);
         double* io3 = d.psi3 + (size_t)b * 4 * epad;
         double* io4 = psi4 + (size_t)b * 4 * epad;
         const double* p1b = d.psi1 + (size_t)b * 4 * epad;
@@ -343,7 +370,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             const Psi x3 = load_psi(io3, epad, e);
             double C, S;
             // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
-            su2_coeffs<1>(a00, a01, g.h01i, dl2, C, S);
+            su2_coeffs<1>(a00, a01, pk, C, S);
             const Psi y3 = su2_apply_w(C, S, x3, su2_w(a00, a01, g.h01i, x3));
             if (d.debug_psi3) {
                 Psi full;
