@@ -65,10 +65,13 @@ __global__ void k_batch_geometry(const Dev* __restrict__ devs, const int2* __res
     geometry_body(devs[a.x], a.y);
 }
 
-// Mixed-precision phases take the single-simulation kernels' register caps
-// (resident warps per SM over spills; see xf_mixed.cu).
+// The batched phases take the single-simulation kernels' register caps for
+// MA (resident warps per SM over spills; see xf_kernels.cu and xf_mixed.cu).
 template <int PREC, int PH>
-constexpr int batch_min_blocks() { return PREC == 0 ? 1 : (PH == xf::PH_A ? 5 : (PH == xf::PH_B ? 6 : 4)); }
+constexpr int batch_min_blocks()
+{
+    return PREC == 0 ? (PH == xf::PH_C ? 3 : 1) : (PH == xf::PH_A ? 5 : (PH == xf::PH_B ? 6 : 4));
+}
 
 template <int PREC, int PH>
 __global__ void __launch_bounds__(256, batch_min_blocks<PREC, PH>()) k_batch_phase(const Dev* __restrict__ devs,

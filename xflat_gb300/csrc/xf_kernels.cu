@@ -67,8 +67,13 @@ __global__ void __launch_bounds__(256) k_phaseB(Dev d)
     fp64::phaseB_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_B));
 }
 
+// Phase C holds fewer values across the energy loop than A and B: capped at
+// 3 (MA) or 4 (MAA) resident blocks per SM it needs at most 80 registers
+// with little or no spilling, and the extra warps hide FP64 latency (measured
+// on GB300: 0.535 -> 0.498 ms at 4.19M MA bins, 1.094 -> 1.024 ms at 8.39M
+// MAA bins; the same caps slow phases A and B).
 template <int GEOM>
-__global__ void __launch_bounds__(256) k_phaseC(Dev d)
+__global__ void __launch_bounds__(256, GEOM == 0 ? 3 : 4) k_phaseC(Dev d)
 {
     pdl_enter();
     fp64::phaseC_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_C));
