@@ -13,11 +13,11 @@ pytestmark = pytest.mark.gpu
 scipy_io = pytest.importorskip("scipy.io")
 
 
-def _cfg(tmp_path, dump_mode=3, **over):
+def _cfg(tmp_path, dump_mode=3, base="config0_ma.txt", **over):
     kv = dict(Abins=8, Ebins=16, R0=20, dr="1e-5", dumpMode=dump_mode, r_step1="0.00005", r_step2="0.00005",
               filePrefix=str(tmp_path) + "/run")
     kv.update(over)
-    return derive("config0_ma.txt", **kv)
+    return derive(base, **kv)
 
 
 def test_dumps_during_run(tmp_path):
@@ -152,8 +152,9 @@ def _files(tmp_path, text, device, iters, k=5):
     return out, st, sim.get_state(0)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_device_control_writes_the_host_loops_files(tmp_path, precision):
+@pytest.mark.parametrize("base,precision", [("config0_ma.txt", "fp64"), ("config0_ma.txt", "mixed"),
+                                            ("config3_maa.txt", "fp64"), ("config3_maa.txt", "mixed")])
+def test_device_control_writes_the_host_loops_files(tmp_path, base, precision):
     """Under device control the step controller evaluates the dump triggers
     and phase A stages the records: the files equal, record for record, those
     of the host-driven loop (radius and iteration triggers, both kinds,
@@ -164,8 +165,10 @@ def test_device_control_writes_the_host_loops_files(tmp_path, precision):
     a_dir, b_dir = tmp_path / "host", tmp_path / "dev"
     a_dir.mkdir()
     b_dir.mkdir()
-    ta = _cfg(a_dir, **over).replace("precision= fp64", "precision= " + precision)
-    tb = _cfg(b_dir, **over).replace("precision= fp64", "precision= " + precision)
+    if base == "config3_maa.txt":
+        over.update(Abins=6, Pbins=3, Ebins=20)
+    ta = _cfg(a_dir, base=base, **over).replace("precision= fp64", "precision= " + precision)
+    tb = _cfg(b_dir, base=base, **over).replace("precision= fp64", "precision= " + precision)
     fa, sa, pa = _files(a_dir, ta, False, 61)
     fb, sb, pb = _files(b_dir, tb, True, 61)
     assert (sa.iterations, sa.accepted) == (sb.iterations, sb.accepted)

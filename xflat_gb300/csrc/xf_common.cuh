@@ -80,23 +80,12 @@ struct BeamH {
     double h00b, h01rb, h01i;
 };
 
-template <int GEOM>
-__device__ __forceinline__ BeamH beam_offsets(const Dev& d, const double* J, int pt, double hm, const BeamIdx& bi)
-{
-    double H[3];
-    beam_hvv<GEOM>(d, J, pt, bi, H);
-    BeamH h;
-    const double a = H[0] + hm;
-    h.h00b = (bi.p & 1) ? -a : a;
-    h.h01rb = (bi.p & 1) ? -H[1] : H[1];
-    h.h01i = H[2];
-    return h;
-}
 
-// Component k of beam_offsets (0: h00 part s (H0 + hm), 1: h01r part s H2,
-// 2: h01i part H3), with the same operations, for lane-parallel per-beam
-// set-up: a warp evaluates one scalar per lane and broadcasts them, instead of
-// every lane evaluating every scalar on the (slow) FP64 pipe.
+// Component k of the beam Hamiltonian offsets (0: the h00 part s (H0 + hm),
+// 1: the h01r part s H2, 2: the h01i part H3) from the moments J at stage
+// point pt (beam_hvv's formula), for lane-parallel per-beam set-up: a warp
+// evaluates one scalar per lane and broadcasts them, instead of every lane
+// evaluating every scalar on the (slow) FP64 pipe.
 __device__ __forceinline__ BeamH shfl_beamh(double v, int first)
 {
     BeamH h;

@@ -239,15 +239,6 @@ __device__ __forceinline__ void ff_add(float hi, float lo, float d, float& nhi, 
     nlo = e - (nhi - s);
 }
 
-__device__ __forceinline__ H3f bin_h(const BeamH& b, float hv0, float hv1)
-{
-    H3f h;
-    h.h00 = hv0 + (float)b.h00b;
-    h.h01r = hv1 + (float)b.h01rb;
-    h.h01i = (float)b.h01i;
-    return h;
-}
-
 // Offset k of the beam Hamiltonian at stage s of phase C: s = 0 the start
 // (J0, point 0), 1 the A1 stage (point 2), 2 the A3 stage (point 1), 3 the B4
 // stage (point 2).  Selected with conditionals so no local array is formed.
@@ -276,22 +267,6 @@ __device__ __forceinline__ H3f shfl_h3(float v, int first)
     h.h01r = __shfl_sync(kFull, v, first + 1);
     h.h01i = __shfl_sync(kFull, v, first + 2);
     return h;
-}
-
-__device__ __forceinline__ H3f diff_beam(const BeamH& a, const BeamH& b)
-{
-    H3f d;
-    d.h00 = (float)(a.h00b - b.h00b);
-    d.h01r = (float)(a.h01rb - b.h01rb);
-    d.h01i = (float)(a.h01i - b.h01i);
-    return d;
-}
-
-// Per-beam energy sum of a stage state = the exact FP64 sum of psi0 (S0) plus
-// the reduced increment sum; lanes own value slots after the reduce-scatter.
-__device__ __forceinline__ double stage_sum(const double* S0, int b, int comp, double inc)
-{
-    return S0[(size_t)b * 4 + comp] + inc;
 }
 
 // ------------------------------------------------------------------ double-float
