@@ -177,3 +177,23 @@ def test_device_control_writes_the_host_loops_files(tmp_path, base, precision):
     for name in fa:
         for v in fa[name]:
             assert np.array_equal(fa[name][v], fb[name][v]), (name, v)
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_unwritable_output_is_reported(tmp_path, device):
+    """Files that cannot be created end the run with XF_EIO and a message
+    naming the file (the reference exits on a NetCDF error, src/IO_f.cpp:88)."""
+    text = _cfg(tmp_path / "missing" / "dir", r_step1="1e-12")
+    sim = xg.Simulation(xg.Config.from_text(text))
+    o = xg._abi.XfRunOpts()
+    sim.lib.xf_run_opts_default(o)
+    o.max_iters = 5
+    o.write_files = 1
+    o.device_control = 1 if device else 0
+    st = xg._abi.XfRunStats()
+    assert sim.lib.xf_run(sim.h, o, xg._abi.XF_STEP_CB(0), None, st) == xg._abi.XF_EIO
+    assert b"cannot create" in sim.lib.xf_last_error(sim.h)
+    assert sim.lib.xf_io_close(sim.h) in (0, xg._abi.XF_EIO)
+    # the handle stays usable
+    out = sim.evolutionLoop(max_iters=3)
+    assert out["iterations"] == 3

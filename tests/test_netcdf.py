@@ -74,3 +74,17 @@ def test_snapshot_read_errors(tmp_path):
     assert lib.xf_snapshot_read(str(empty).encode(), -1, None, None, None, ctypes.byref(n)) == 0 and n.value == 0
     with scipy_io.netcdf_file(str(empty), "r", mmap=False) as f:
         assert f.variables["psi"].shape[0] == 0
+
+
+def test_truncated_snapshot_is_an_io_error(tmp_path):
+    cfg = xg.Config.from_text(derive("config0_ma.txt", Abins=3, Ebins=5))
+    psi = np.random.default_rng(1).normal(size=(2, 3, 4, 4, 5))
+    path = tmp_path / "t.nc"
+    assert _write(path, cfg, np.ascontiguousarray(psi), np.array([1.0, 2.0]), np.array([.1, .2])) == 0
+    data = path.read_bytes()
+    lib = _abi.load()
+    out = np.empty(psi[0].size)
+    for cut in (len(data) - 8, len(data) // 2, 40, 3):
+        path.write_bytes(data[:cut])
+        rc = lib.xf_snapshot_read(str(path).encode(), -1, None, None, out.ctypes.data_as(dp), None)
+        assert rc == _abi.XF_EIO, cut
