@@ -97,7 +97,7 @@ int xf_handle::init(const xf_config& c)
     ne = cfg.ebins;
     epad = (ne + 31) / 32 * 32;
     nbeams = A * P * 4;
-    shape = xf::default_shape(nbeams, epad);
+    shape = xf::default_shape(nbeams, epad, cfg.precision == XF_PREC_MIXED);
     XF_CUDA(this, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     for (int i = 0; i < 7; ++i) XF_CUDA(this, cudaEventCreate(&ev[i]));
 
@@ -680,11 +680,14 @@ int xf_set_option(xf_handle* h, const char* name, double value)
         h->shape.threads = t ? t : 256;
         const int cap = xf::max_phase_blocks(h->nbeams, 32);
         h->shape.blocks = std::min(h->shape.blocks, std::max(1, cap));
+        h->shape.blocks_ab = std::min(h->shape.blocks_ab, std::max(1, cap));
     } else if (n == "blocks") {
         const int b = (int)value;
         const int cap = std::max(xf::max_phase_blocks(h->nbeams, 256), 152 * 4);
         if (b < 0 || b > cap) return h->fail(XF_EINVAL, "blocks out of range");
-        h->shape.blocks = b ? b : xf::default_shape(h->nbeams, h->epad).blocks;
+        const xf::Shape def = xf::default_shape(h->nbeams, h->epad, h->mixed != nullptr);
+        h->shape.blocks = b ? b : def.blocks;
+        h->shape.blocks_ab = b ? b : def.blocks_ab;
     } else {
         return h->fail(XF_EINVAL, "unknown option " + n);
     }

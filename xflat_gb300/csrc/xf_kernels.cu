@@ -209,12 +209,18 @@ int max_phase_blocks(int nbeams, int threads)
     return std::max(1, std::min(need, 152 * 16));
 }
 
-Shape default_shape(int nbeams, int epad)
+// The mixed-precision phases A and B run best as a single wave of resident
+// blocks (5 per SM; measured on GB300: 0.054 / 0.037 ms at 4.19M MA bins
+// with 760 blocks against 0.058 / 0.040 with one block per 8 beams, 0.130 /
+// 0.093 against 0.152 / 0.099 at 8.39M MAA bins); phase C, and the FP64
+// phases, limited by the FP64 pipe, with one block per 8 beams.
+Shape default_shape(int nbeams, int epad, bool mixed)
 {
     (void)epad;
     Shape s;
     s.threads = 256;
     s.blocks = max_phase_blocks(nbeams, s.threads);
+    s.blocks_ab = mixed ? std::min(s.blocks, 152 * 5) : s.blocks;
     return s;
 }
 

@@ -10,11 +10,12 @@ namespace xf {
 struct Shape {
     int threads = 256;   // threads per block (multiple of 32)
     int blocks = 0;      // grid size of the phase kernels
+    int blocks_ab = 0;   // mixed precision: grid size of phases A and B (0: blocks)
 };
 
 // Grid-size limit used to size the partial-sum buffer.
 int max_phase_blocks(int nbeams, int threads);
-Shape default_shape(int nbeams, int epad);
+Shape default_shape(int nbeams, int epad, bool mixed = false);
 
 void launch_geometry(const Dev& d, cudaStream_t st);
 void launch_esum(const Dev& d, const double* psi, double* S, cudaStream_t st);

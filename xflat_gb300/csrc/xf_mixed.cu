@@ -240,13 +240,14 @@ int mixed_get_state(xf_handle* h, Mixed* m, int which, double* psi)
 
 void mixed_launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
 {
+    const int ab = sh.blocks_ab > 0 ? sh.blocks_ab : sh.blocks;
     if (d.geom == 0) {
-        if (phase == PH_A) launch_pdl(k_mixA<0>, sh.blocks, sh.threads, st, d);
-        else if (phase == PH_B) launch_pdl(k_mixB<0>, sh.blocks, sh.threads, st, d);
+        if (phase == PH_A) launch_pdl(k_mixA<0>, ab, sh.threads, st, d);
+        else if (phase == PH_B) launch_pdl(k_mixB<0>, ab, sh.threads, st, d);
         else launch_pdl(k_mixC<0>, sh.blocks, sh.threads, st, d);
     } else {
-        if (phase == PH_A) launch_pdl(k_mixA<1>, sh.blocks, sh.threads, st, d);
-        else if (phase == PH_B) launch_pdl(k_mixB<1>, sh.blocks, sh.threads, st, d);
+        if (phase == PH_A) launch_pdl(k_mixA<1>, ab, sh.threads, st, d);
+        else if (phase == PH_B) launch_pdl(k_mixB<1>, ab, sh.threads, st, d);
         else launch_pdl(k_mixC<1>, sh.blocks, sh.threads, st, d);
     }
 }
