@@ -53,16 +53,20 @@ __device__ __forceinline__ RedTarget tile_target(const Dev& d, const Tile& t, in
     rt.idx = t.idx;
     rt.count = t.count;
     rt.ticket = &d.ctl->ticket[phase];
+    rt.gticket = d.gticket + phase * xf::kMaxRedGroups;
     return rt;
 }
 
-__global__ void k_batch_geometry(const Dev* __restrict__ devs, const int2* __restrict__ angles, int n)
+// Blocks of 32 work-list angles x 3 stage points (geometry_point); the
+// angles of one block may belong to different instances.
+__global__ void __launch_bounds__(96) k_batch_geometry(const Dev* __restrict__ devs, const int2* __restrict__ angles, int n)
 {
     xf::pdl_enter();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int2 a = angles[i];
-    geometry_body(devs[a.x], a.y);
+    __shared__ double s_c[96];
+    const int slot = threadIdx.x % 32, pt = threadIdx.x / 32;
+    const int i = blockIdx.x * 32 + slot;
+    const int2 a = i < n ? angles[i] : make_int2(0, -1);
+    geometry_point(devs[a.x], a.y, pt, slot, 32, s_c);
 }
 
 // The batched phases take the single-simulation kernels' register caps for
@@ -194,7 +198,9 @@ int build_lists(xf_batch* b, int warps)
         for (int t = 0; t < ntti; ++t) tt.push_back(Tile{i, t * 256, t, ntti});
         for (int a = 0; a < h->A; ++a) ang.push_back(make_int2(i, a));
         part_off[i] = part_total;
-        part_total += (size_t)std::max(nwti, ntti) * xf::kPartStride;
+        if (std::max(nwti, ntti) > xf::kRedGroup * xf::kMaxRedGroups)
+            return b->fail(XF_EUNSUPPORTED, "instance " + std::to_string(i) + ": too many tiles for the reduction");
+        part_total += (size_t)xf::red_rows(std::max(nwti, ntti)) * xf::kPartStride;
     }
     if (b->d_part) cudaFree(b->d_part);
     if (b->d_wtiles) cudaFree(b->d_wtiles);
@@ -234,7 +240,7 @@ void launch_iteration(xf_batch* b)
     const int threads = 32 * b->warps;
     const Dev* dv = b->d_devs;
     const Tile* wt = b->d_wtiles;
-    xf::launch_pdl(k_batch_geometry, (b->nang + 127) / 128, 128, b->st, dv, (const int2*)b->d_angles, b->nang);
+    xf::launch_pdl(k_batch_geometry, (b->nang + 31) / 32, 96, b->st, dv, (const int2*)b->d_angles, b->nang);
     if (b->prec == XF_PREC_MIXED) {
         xf::launch_pdl(k_batch_renorm, b->nwt, threads, b->st, dv, wt);
         xf::launch_pdl(k_batch_moments, b->ntt, 256, b->st, dv, (const Tile*)b->d_ttiles);

@@ -188,13 +188,16 @@ __device__ __forceinline__ int comp_of(int k) { return k == 0 ? 0 : (k == 1 ? 2 
 // block, with s_out[0..nused*K) holding the grid totals and s_out[31] the grid
 // maximum of `mx` (ignored unless with_max).
 // Where a group of blocks reduces its per-block partials: the block's slot
-// `idx` of `count` slots at `partials`, and the ticket that elects the last
-// block of the group (single simulation: the grid; batch: one instance's tiles).
+// `idx` of `count` slots at `partials` (followed by room for the group sums,
+// red_rows(count) rows in all), the tickets that elect the last block of each
+// group of kRedGroup slots (`gticket`, one per group) and the last group
+// (`ticket`).  Single simulation: the grid; batch: one instance's tiles.
 struct RedTarget {
     double* partials;
     int idx;
     int count;
     unsigned int* ticket;
+    unsigned int* gticket;
 };
 
 template <int K>
@@ -226,6 +229,33 @@ __device__ inline bool group_reduce_split(const RedTarget& rt, int G, int nused,
     return group_reduce_tail<K>(rt, nused, mx, with_max, s_warp, s_out);
 }
 
+// Sums rows [0, n) of `rows` (row stride kPartStride) slot by slot: slots
+// [0, nout) by addition and, with with_max, slot 31 by maximum.  Warp w takes
+// rows w, w + nw, ... (lane = slot), then the warps' sums are combined in warp
+// order, so the result depends only on n and the block size.  Leaves the
+// totals in s_out[0..32).
+__device__ inline void sum_rows(const double* rows, int n, int nout, bool with_max, double* s_warp, double* s_out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const bool is_max = with_max && lane == 31;
+    double t = is_max ? -1.0 : 0.;
+    if (lane < nout || is_max) {
+        for (int j = warp; j < n; j += nw) {
+            const double x = __ldcg(rows + (size_t)j * kPartStride + lane);
+            t = is_max ? fmax(t, x) : t + x;
+        }
+    }
+    __syncthreads();  // s_warp may still be read by the caller's block-partial pass
+    s_warp[warp * 32 + lane] = t;
+    __syncthreads();
+    if (warp == 0) {
+        double a = s_warp[lane];
+        for (int w = 1; w < nw; ++w) a = is_max ? fmax(a, s_warp[w * 32 + lane]) : a + s_warp[w * 32 + lane];
+        s_out[lane] = a;
+    }
+    __syncthreads();
+}
+
 template <int K>
 __device__ inline bool group_reduce_tail(const RedTarget& rt, int nused, double mx, bool with_max, double* s_warp,
                                          double* s_out)
@@ -247,52 +277,35 @@ __device__ inline bool group_reduce_tail(const RedTarget& rt, int nused, double 
     }
     __threadfence();
     __syncthreads();
+    // level 1: the last block of this group of kRedGroup partials sums the group
+    const int g = rt.idx / kRedGroup, ng = (rt.count + kRedGroup - 1) / kRedGroup;
+    const int g0 = g * kRedGroup, gsize = min(kRedGroup, rt.count - g0);
     __shared__ int s_last;
     if (threadIdx.x == 0) {
-        const unsigned t = atomicAdd(rt.ticket, 1u);
-        s_last = (t == (unsigned)rt.count - 1);
+        const unsigned t = atomicAdd(&rt.gticket[g], 1u);
+        s_last = (t == (unsigned)gsize - 1);
     }
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
-    // Last block: thread t sums blocks t, t+bs, ... for every slot, then the
-    // block reduces the 32 slots with a reduce-scatter per warp.
-    double vals[32];
-#pragma unroll
-    for (int k = 0; k < 32; ++k) vals[k] = 0.;
-    double m = -1.0;
-    for (int b = threadIdx.x; b < rt.count; b += blockDim.x) {
-        const double* pb = rt.partials + (size_t)b * kPartStride;
-#pragma unroll
-        for (int k = 0; k < 31; ++k)
-            if (k < nout) vals[k] += __ldcg(pb + k);
-        if (with_max) m = fmax(m, __ldcg(pb + 31));
-    }
-    warp_reduce_scatter<32>(vals, lane);
+    if (threadIdx.x == 0) rt.gticket[g] = 0u;
+    sum_rows(rt.partials + (size_t)g0 * kPartStride, gsize, nout, with_max, s_warp, s_out);
+    if (ng == 1) return true;
+    // level 2: the group sum goes after the block partials; the last group sums them
+    double* gpart = rt.partials + (size_t)rt.count * kPartStride;
+    if ((int)threadIdx.x < 32 && ((int)threadIdx.x < nout || (with_max && threadIdx.x == 31)))
+        gpart[(size_t)g * kPartStride + threadIdx.x] = s_out[threadIdx.x];
+    __threadfence();
     __syncthreads();
-    s_warp[warp * 32 + lane] = vals[0];
-    if (with_max) {
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) m = fmax(m, __shfl_xor_sync(kFull, m, off));
+    if (threadIdx.x == 0) {
+        const unsigned t = atomicAdd(rt.ticket, 1u);
+        s_last = (t == (unsigned)ng - 1);
     }
     __syncthreads();
-    if ((int)threadIdx.x < nout) {
-        double t = 0.;
-        for (int w = 0; w < nw; ++w) t += s_warp[w * 32 + threadIdx.x];
-        s_out[threadIdx.x] = t;
-    }
-    if (with_max) {
-        __shared__ double s_m[32];
-        if (lane == 0) s_m[warp] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double mm = s_m[0];
-            for (int w = 1; w < nw; ++w) mm = fmax(mm, s_m[w]);
-            s_out[31] = mm;
-        }
-    }
+    if (!s_last) return false;
+    __threadfence();
     if (threadIdx.x == 0) *rt.ticket = 0u;
-    __syncthreads();
+    sum_rows(gpart, ng, nout, with_max, s_warp, s_out);
     return true;
 }
 
@@ -483,6 +496,7 @@ __device__ __forceinline__ RedTarget grid_target(const Dev& d, int phase)
     rt.idx = blockIdx.x;
     rt.count = gridDim.x;
     rt.ticket = &d.ctl->ticket[phase];
+    rt.gticket = d.gticket + phase * kMaxRedGroups;
     return rt;
 }
 }  // namespace detail
@@ -491,10 +505,6 @@ __device__ __forceinline__ RedTarget grid_target(const Dev& d, int phase)
 namespace xf {
 namespace detail {
 
-// phy::calcAngleBins at r, r+dr/2, r+dr and phy::calcDeltaLs for the three
-// path segments (src/Nmr.cpp:153-173, src/Phy_MA.cpp:172-227,
-// src/Phy_MAA.cpp:194-241) for angle bin `ang`.  Under device control angle 0
-// also evaluates the matter term at the three points (src/Matt.cpp:31-64).
 // Mirrors entry i of the geometry table as a double-float pair (mixed path).
 __device__ __forceinline__ void geo_store(const Dev& d, int i, double v)
 {
@@ -506,65 +516,64 @@ __device__ __forceinline__ void geo_store(const Dev& d, int i, double v)
     }
 }
 
-__device__ inline void geometry_body(const Dev& d, int ang)
+// phy::calcAngleBins at r, r+dr/2, r+dr and phy::calcDeltaLs for the three
+// path segments (src/Nmr.cpp:153-173, src/Phy_MA.cpp:172-227,
+// src/Phy_MAA.cpp:194-241), one thread per (angle bin, stage point): the
+// thread of point pt evaluates cos, sin and the weight at r_pt and the path
+// length of segment pt, which needs the cosines of two points; the block
+// exchanges them through s_c[3][nslots] (slot = the angle's place in the
+// block).  Every thread of the block must call it (it synchronises the
+// block); ang < 0 marks a thread without an angle.  Under device control the
+// threads of angle 0 also evaluate the matter term at their point
+// (src/Matt.cpp:31-64).
+__device__ inline void geometry_point(const Dev& d, int ang, int pt, int slot, int nslots, double* s_c)
 {
-    Ctl* ctl = d.ctl;
-    if (ctl->done) return;
-    const double r = ctl->r, dr = ctl->dr;
-    const double dr2 = .5 * dr;
-    const double rdr = r + dr;
-    const double rdr2 = r + dr2;
-    const double rp[3] = {r, rdr2, rdr};
-    if (d.device_control && ang == 0) {
-#pragma unroll
-        for (int pt = 0; pt < 3; ++pt) {
+    const bool live = ang >= 0 && !d.ctl->done;
+    double dr = 0., dr2 = 0.;
+    if (live) {
+        Ctl* ctl = d.ctl;
+        const double r = ctl->r;
+        dr = ctl->dr;
+        dr2 = .5 * dr;
+        const double rp = pt == 0 ? r : (pt == 1 ? r + dr2 : r + dr);
+        if (d.device_control && ang == 0) {
             double hm = 0.;
             if (d.has_matter) {
-                const double R = 10. / rp[pt];
+                const double R = 10. / rp;
                 const double far = d.nbfar * (R * R * R);
-                const double near = d.nb0 * exp((d.Rv - rp[pt]) / d.hNS);
+                const double near = d.nb0 * exp((d.Rv - rp) / d.hNS);
                 hm = d.mat_coeff * (far + near) * .5;
             }
             ctl->hm[pt] = hm;
         }
-    }
-    if (ang >= d.A) return;
-    if (d.sa) {
-        // SA (src/Phy_SA.cpp:121-147, 250-256): no angular dependence, dl =
-        // dr/2, dr, dr/2, and H = kappa D(r) N.  Stored in the MA layout as
-        // cos = 0 and weight D(r), so the MA moment J0 = sum_b w N_b gives
-        // H = kappa (J0 - cos J1) = kappa D(r) N.
-#pragma unroll
-        for (int pt = 0; pt < 3; ++pt) {
-            const double R = d.Rv / rp[pt];
+        if (d.sa) {
+            // SA (src/Phy_SA.cpp:121-147, 250-256): no angular dependence, dl =
+            // dr/2, dr, dr/2, and H = kappa D(r) N.  Stored in the MA layout as
+            // cos = 0 and weight D(r), so the MA moment J0 = sum_b w N_b gives
+            // H = kappa (J0 - cos J1) = kappa D(r) N.
+            const double R = d.Rv / rp;
             const double tm = 1. - sqrt(1. - (R * R));
             geo_store(d, geo_idx(0, pt, ang, d.A), 0.);
             geo_store(d, geo_idx(1, pt, ang, d.A), 0.);
             geo_store(d, geo_idx(2, pt, ang, d.A), .5 * (tm * tm));
+            geo_store(d, geo_idx(3, pt, ang, d.A), pt == 1 ? dr : dr2);
+        } else {
+            const double ra = d.Rv / rp;
+            const double r2 = ra * ra;
+            const double c = sqrt(1. - r2 * (1. - d.cos2R[ang]));
+            geo_store(d, geo_idx(0, pt, ang, d.A), c);
+            geo_store(d, geo_idx(1, pt, ang, d.A), ra * d.sinR[ang]);
+            geo_store(d, geo_idx(2, pt, ang, d.A), .5 * (1. / c) * r2 * d.dcos2R[ang]);
+            s_c[pt * nslots + slot] = c;
         }
-        geo_store(d, geo_idx(3, 0, ang, d.A), dr2);
-        geo_store(d, geo_idx(3, 1, ang, d.A), dr);
-        geo_store(d, geo_idx(3, 2, ang, d.A), dr2);
-        return;
     }
-    double c[3];
-#pragma unroll
-    for (int pt = 0; pt < 3; ++pt) {
-        const double ra = d.Rv / rp[pt];
-        const double r2 = ra * ra;
-        c[pt] = sqrt(1. - r2 * (1. - d.cos2R[ang]));
-        geo_store(d, geo_idx(0, pt, ang, d.A), c[pt]);
-        geo_store(d, geo_idx(1, pt, ang, d.A), ra * d.sinR[ang]);
-        geo_store(d, geo_idx(2, pt, ang, d.A), .5 * (1. / c[pt]) * r2 * d.dcos2R[ang]);
-    }
-    if (d.geom == 0) {
-        geo_store(d, geo_idx(3, 0, ang, d.A), dr2 / (c[0]));
-        geo_store(d, geo_idx(3, 1, ang, d.A), dr / (c[0]));
-        geo_store(d, geo_idx(3, 2, ang, d.A), dr2 / (c[1]));
-    } else {
-        geo_store(d, geo_idx(3, 0, ang, d.A), dr2 / ((c[0] + c[1]) * .5));
-        geo_store(d, geo_idx(3, 1, ang, d.A), dr / ((c[0] + c[2]) * .5));
-        geo_store(d, geo_idx(3, 2, ang, d.A), dr2 / ((c[1] + c[2]) * .5));
+    __syncthreads();
+    if (live && !d.sa) {
+        const double c0 = s_c[slot], c1 = s_c[nslots + slot], c2 = s_c[2 * nslots + slot];
+        double dl;
+        if (d.geom == 0) dl = pt == 0 ? dr2 / (c0) : (pt == 1 ? dr / (c0) : dr2 / (c1));
+        else dl = pt == 0 ? dr2 / ((c0 + c1) * .5) : (pt == 1 ? dr / ((c0 + c2) * .5) : dr2 / ((c1 + c2) * .5));
+        geo_store(d, geo_idx(3, pt, ang, d.A), dl);
     }
 }
 

@@ -21,6 +21,13 @@ namespace xf {
 
 constexpr int kNJ = 16;        // moment slots: MA uses J0[4], J1[4]; MAA J0, Jx, Jy, Jz [4] each
 constexpr int kPartStride = 32;  // doubles per block in the partial-sum buffer
+// Block partials are reduced in two levels: the last block of each group of
+// kRedGroup consecutive partials sums the group, and the last group sums the
+// group sums (stored after the block partials).
+constexpr int kRedGroup = 32;
+constexpr int kMaxRedGroups = 1024;  // groups per reduction (group tickets per phase)
+// Rows of the partial-sum buffer for `count` block partials and their group sums.
+__host__ __device__ constexpr int red_rows(int count) { return count + (count + kRedGroup - 1) / kRedGroup; }
 
 enum Phase { PH_A = 0, PH_B = 1, PH_C = 2, PH_MOM = 3 };
 
@@ -114,7 +121,8 @@ struct Dev {
                           // J ~ 1e50 are outside FP32's range; kappa J, the Hamiltonian scale, is not)
     double* psi1;
     double* psi3;
-    double* partials;     // [grid][kPartStride]
+    double* partials;     // [red_rows(grid)][kPartStride]
+    unsigned int* gticket;  // [4 phases][kMaxRedGroups] group tickets of the two-level reduction
     double* log;          // accepted-step log [cap][3] (device control), may be null
     long long log_cap;
     Ctl* ctl;

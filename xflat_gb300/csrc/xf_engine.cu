@@ -134,7 +134,8 @@ int xf_handle::init(const xf_config& c)
         if ((rc = dalloc(this, &d_phif, pf.size())) || (rc = upload(this, d_phif, pf))) return rc;
     }
     const int maxblk = std::max(xf::max_phase_blocks(nbeams, 256), 152 * 4);
-    if ((rc = dalloc(this, &d_partials, (size_t)maxblk * xf::kPartStride))) return rc;
+    if ((rc = dalloc(this, &d_partials, (size_t)xf::red_rows(maxblk) * xf::kPartStride))) return rc;
+    if ((rc = dalloc(this, &d_gticket, 4 * (size_t)xf::kMaxRedGroups))) return rc;
     if ((rc = dalloc(this, &d_ctl, 1))) return rc;
     if ((rc = dalloc(this, &d_hvv, 4 * (size_t)A * P))) return rc;
     if ((rc = dalloc(this, &d_Sscratch, 4 * (size_t)nbeams))) return rc;
@@ -162,6 +163,7 @@ int xf_handle::init(const xf_config& c)
     dev.cosphif = d_phif;
     dev.sinphif = d_phif + 2 * cphi.size();
     dev.partials = d_partials;
+    dev.gticket = d_gticket;
     dev.ctl = d_ctl;
     for (int p = 0; p < 4; ++p) dev.LE[p] = tab.LE[p];
     dev.kappa = tab.integ_coef;
@@ -218,6 +220,7 @@ void xf_handle::release()
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (d_geof) cudaFree(d_geof);
+    if (d_gticket) cudaFree(d_gticket);
     if (d_phif) cudaFree(d_phif);
     if (d_ctl) cudaFree(d_ctl);
     if (h_ctl) cudaFreeHost(h_ctl);

@@ -36,6 +36,7 @@ struct xf_handle {
     float* d_geof = nullptr;     // geometry table as double-float (mixed path)
     float* d_phif = nullptr;     // [4][P]: cos(phi) hi, lo, sin(phi) hi, lo
     double* d_partials = nullptr;
+    unsigned int* d_gticket = nullptr;  // [4][kMaxRedGroups]
     double* d_hvv = nullptr;
     double* d_Sscratch = nullptr;
     double* d_psi[4] = {};  // storage for psi0, psi1, psi3, psi4 (roles of 0 and 3 swap)

@@ -41,12 +41,21 @@ using namespace detail;
 
 // phy::calcAngleBins at r, r+dr/2, r+dr and phy::calcDeltaLs for the three
 // path segments (src/Nmr.cpp:153-173, src/Phy_MA.cpp:172-227,
-// src/Phy_MAA.cpp:194-241).  Under device control thread 0 also evaluates the
-// matter term at the three points (src/Matt.cpp:31-64).
-__global__ void k_geometry(Dev d)
+// src/Phy_MAA.cpp:194-241).  Under device control the threads of angle 0 also
+// evaluate the matter term at the three points (src/Matt.cpp:31-64).  Blocks
+// of kGeoAngles angle bins x 3 stage points (geometry_point): the square roots
+// and divisions of one angle run on three threads, and the launch spreads
+// over A/32 SMs (one thread per angle on 128-thread blocks took 13 us per
+// launch at A = 256 on GB300, FP64-pipe bound on two SMs).
+constexpr int kGeoAngles = 32;
+
+__global__ void __launch_bounds__(3 * kGeoAngles) k_geometry(Dev d)
 {
     pdl_enter();
-    geometry_body(d, blockIdx.x * blockDim.x + threadIdx.x);
+    __shared__ double s_c[3 * kGeoAngles];
+    const int slot = threadIdx.x % kGeoAngles, pt = threadIdx.x / kGeoAngles;
+    const int ang = blockIdx.x * kGeoAngles + slot;
+    geometry_point(d, ang < d.A ? ang : -1, pt, slot, kGeoAngles, s_c);
 }
 
 // ------------------------------------------------------------------ phases
@@ -226,8 +235,7 @@ Shape default_shape(int nbeams, int epad, bool mixed)
 
 void launch_geometry(const Dev& d, cudaStream_t st)
 {
-    const int t = 128;
-    launch_pdl(k_geometry, (d.A + t - 1) / t, t, st, d);
+    launch_pdl(k_geometry, (d.A + kGeoAngles - 1) / kGeoAngles, 3 * kGeoAngles, st, d);
 }
 
 void launch_esum(const Dev& d, const double* psi, double* S, cudaStream_t st)
