@@ -101,6 +101,8 @@ typedef struct xf_run_stats {
     double device_ms;      /* CUDA-event time of the loop on the handle's stream */
     long kernel_launches;  /* device kernels launched by this call */
     long log_len;          /* accepted-step records written to opts->log */
+    long h2d_bytes;        /* host-to-device bytes this call copied (inputs, control block) */
+    long d2h_bytes;        /* device-to-host bytes this call copied (control, Max_err, log, output records) */
 } xf_run_stats;
 
 /* Defaults: max_iters -1, device_control 0, iters_per_launch 16, r0/dr0 NaN. */

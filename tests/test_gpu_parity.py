@@ -162,6 +162,20 @@ def test_device_control_equals_host_loop():
     np.testing.assert_array_equal(a["log"], b["log"])
     assert a["r_end"] == b["r_end"] and a["dr_end"] == b["dr_end"]
     assert np.array_equal(s1.get_state(0), s2.get_state(0))
+    # copies the loops report: host-driven r, dr, hm H2D (40 B) and Max_err D2H
+    # (8 B) per iteration, plus the log (24 B per record); device control one
+    # control-block copy per launch of 16 iterations
+    it = a["iterations"]
+    assert a["h2d_bytes"] >= 40 * it and a["d2h_bytes"] >= 8 * it + 24 * a["log_len"]
+    ctl = b["d2h_bytes"] - 24 * b["log_len"]
+    assert 0 < b["h2d_bytes"] < 40 * it and 0 < ctl
+    # the same 48 iterations in 3 and in 6 launches: 3 more control-block copies
+    c = s2.evolutionLoop(max_iters=48, device_control=True, iters_per_launch=16)
+    d = s2.evolutionLoop(max_iters=48, device_control=True, iters_per_launch=8)
+    assert c["iterations"] == d["iterations"] == 48
+    assert c["h2d_bytes"] == d["h2d_bytes"]
+    extra = d["d2h_bytes"] - c["d2h_bytes"]
+    assert extra > 0 and extra % 3 == 0 and c["d2h_bytes"] >= extra
 
 
 def test_bitwise_reproducible():

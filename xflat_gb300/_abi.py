@@ -53,6 +53,7 @@ class XfRunStats(ctypes.Structure):
         ("r_end", ctypes.c_double), ("dr_end", ctypes.c_double),
         ("seconds", ctypes.c_double), ("last_max_err", ctypes.c_double), ("device_ms", ctypes.c_double),
         ("kernel_launches", ctypes.c_long), ("log_len", ctypes.c_long),
+        ("h2d_bytes", ctypes.c_long), ("d2h_bytes", ctypes.c_long),
     ]
 
 

@@ -243,6 +243,7 @@ int xf_handle::pull_ctl()
 {
     XF_CUDA(this, cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     XF_CUDA(this, cudaStreamSynchronize(st));
+    d2h_bytes += sizeof(Ctl);
     return XF_OK;
 }
 
@@ -290,6 +291,7 @@ int xf_handle::push_inputs(double r, double dr)
     h_in[3] = xf::matter_hm(cfg, tab, r + dr2);
     h_in[4] = xf::matter_hm(cfg, tab, r + dr);
     XF_CUDA(this, cudaMemcpyAsync(&d_ctl->r, h_in, 5 * sizeof(double), cudaMemcpyHostToDevice, st));
+    h2d_bytes += 5 * sizeof(double);
     return XF_OK;
 }
 
@@ -329,6 +331,7 @@ int xf_handle::step(double r, double dr, double* max_err)
     launches += 4;
     XF_CUDA(this, cudaMemcpyAsync(&h_ctl->max_err, &d_ctl->max_err, sizeof(double), cudaMemcpyDeviceToHost, st));
     XF_CUDA(this, cudaStreamSynchronize(st));
+    d2h_bytes += sizeof(double);
     if (time_phases) {
         float ms;
         for (int i = 0; i < 3; ++i) {
@@ -510,6 +513,7 @@ int xf_handle::start_device_run(double r, double dr, long Ts, bool files)
     if (files) io_dev_fill(h_ctl);
     XF_CUDA(this, cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
     XF_CUDA(this, cudaStreamSynchronize(st));
+    h2d_bytes += sizeof(Ctl);
     return XF_OK;
 }
 
@@ -566,6 +570,7 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         }
         const long long ran = h_ctl->iters - prev_iters;
         launches += 4 * ran;
+        d2h_bytes += sizeof(Ctl);  // the graph's copy of the control block
         if (o.time_phases) {
             for (long long i = 0; i < ran && i < kk; ++i)
                 for (int ph = 0; ph < 3; ++ph) {
@@ -598,6 +603,7 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     if (o.log && h_ctl->log_len > 0) {
         const long n = (long)std::min<long long>(h_ctl->log_len, o.log_cap);
         XF_CUDA(this, cudaMemcpy(o.log, d_log, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+        d2h_bytes += 3 * (long long)n * sizeof(double);
         s.log_len = n;
     }
     j0_valid = true;
@@ -805,6 +811,7 @@ int xf_run(xf_handle* h, const xf_run_opts* opts, xf_step_cb cb, void* user, xf_
     xf_run_stats s;
     std::memset(&s, 0, sizeof(s));
     h->launches = 0;
+    h->h2d_bytes = h->d2h_bytes = 0;
     h->time_phases = o.time_phases;
     for (int i = 0; i < 3; ++i) {
         h->phase_ms[i] = 0.;
@@ -819,6 +826,8 @@ int xf_run(xf_handle* h, const xf_run_opts* opts, xf_step_cb cb, void* user, xf_
     }
     h->time_phases = 0;
     s.kernel_launches = h->launches;
+    s.h2d_bytes = h->h2d_bytes;
+    s.d2h_bytes = h->d2h_bytes;
     if (stats) *stats = s;
     return rc;
 }

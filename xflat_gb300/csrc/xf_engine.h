@@ -63,6 +63,7 @@ struct xf_handle {
     double phase_ms[3] = {0., 0., 0.};
     long phase_n[3] = {0, 0, 0};
     long launches = 0;
+    long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes copied by the current xf_run
     std::string err;
 
     struct GraphEntry {

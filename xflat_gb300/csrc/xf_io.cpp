@@ -419,6 +419,7 @@ int write_snapshot(xf_handle* h, double r, double dr)
         unclaim(io, io.busy_state, b);
         return rc;
     }
+    h->d2h_bytes += (long long)h->nbeams * 4 * h->ne * sizeof(double);
     io.itr++;
     enqueue(io, Job{JOB_SNAP, b, r, dr, c.sync_step > 0 && io.itr % c.sync_step == 0});
     io.next_state = (io.next_state + 1) % kStateBufs;
@@ -444,6 +445,7 @@ int write_probability(xf_handle* h, double r)
         unclaim(io, io.busy_surv, b);
         return rc;
     }
+    h->d2h_bytes += (long long)h->nbeams * sizeof(double);
     const int64_t ss = h->cfg.sync_step;
     enqueue(io, Job{JOB_PROB, b, r, 0., ss > 0 && io.itr % ss == 0});
     io.next_surv = (io.next_surv + 1) % kSurvBufs;
@@ -553,6 +555,7 @@ int xf_handle::io_dev_drain(long long count, long long staged_in, bool final)
     std::vector<xf::IoRec> ring(io->nslots);
     if (cudaMemcpy(ring.data(), io->d_log, ring.size() * sizeof(xf::IoRec), cudaMemcpyDeviceToHost) != cudaSuccess)
         return fail(XF_ECUDA, "reading the output records failed");
+    d2h_bytes += (long long)ring.size() * sizeof(xf::IoRec);
     const size_t snap = (size_t)nbeams * 4 * ne;
     for (long long n = io->dev_done; n < staged; ++n) {
         const xf::IoRec& rec = ring[n % io->nslots];
@@ -570,6 +573,7 @@ int xf_handle::io_dev_drain(long long count, long long staged_in, bool final)
                 return fail(XF_ECUDA, std::string("output copy: ") + cudaGetErrorString(e));
             }
             io->snap_pend[rec.snap_slot] = 1;
+            d2h_bytes += (long long)snap * sizeof(double);
             io->itr++;
             enqueue(*io, Job{JOB_SNAP, b, rec.r, rec.dr, rec.sync_snap != 0});
             io->next_state = (io->next_state + 1) % kStateBufs;
@@ -587,6 +591,7 @@ int xf_handle::io_dev_drain(long long count, long long staged_in, bool final)
                 return fail(XF_ECUDA, std::string("output copy: ") + cudaGetErrorString(e));
             }
             io->prob_pend[rec.prob_slot] = 1;
+            d2h_bytes += (long long)nbeams * sizeof(double);
             enqueue(*io, Job{JOB_PROB, b, rec.r, 0., rec.sync_prob != 0});
             io->next_surv = (io->next_surv + 1) % kSurvBufs;
         }
@@ -612,6 +617,7 @@ int xf_handle::io_dev_end()
     if (cudaMemcpyAsync(d_ctl, h_ctl, sizeof(xf::Ctl), cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return fail(XF_ECUDA, "control block upload failed");
+    h2d_bytes += sizeof(xf::Ctl);
     return flush_files();
 }
 
