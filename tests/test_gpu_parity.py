@@ -163,10 +163,11 @@ def test_device_control_equals_host_loop():
     assert a["r_end"] == b["r_end"] and a["dr_end"] == b["dr_end"]
     assert np.array_equal(s1.get_state(0), s2.get_state(0))
     # copies the loops report: host-driven r, dr, hm H2D (40 B) and Max_err D2H
-    # (8 B) per iteration, plus the log (24 B per record); device control one
-    # control-block copy per launch of 16 iterations
+    # (8 B) per iteration (its log is written on the host); device control one
+    # control-block copy per launch of 16 iterations, plus the log (24 B per
+    # record)
     it = a["iterations"]
-    assert a["h2d_bytes"] >= 40 * it and a["d2h_bytes"] >= 8 * it + 24 * a["log_len"]
+    assert a["h2d_bytes"] >= 40 * it and a["d2h_bytes"] >= 8 * it
     ctl = b["d2h_bytes"] - 24 * b["log_len"]
     assert 0 < b["h2d_bytes"] < 40 * it and 0 < ctl
     # the same 48 iterations in 3 and in 6 launches: 3 more control-block copies

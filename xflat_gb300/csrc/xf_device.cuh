@@ -137,6 +137,7 @@ struct Dev {
     int device_control;   // phase C runs the accept/reject/dr controller
     int renorm_every;     // mixed precision: renormalise psi0 every this many accepted steps
     int debug_psi3;       // phase C also stores U(h4, dl2) psi3 into psi3 (the reference's S10 result)
+    int prefetch;         // mixed precision: L1 prefetch distance of the state rows, in energy-loop iterations
 };
 
 // Geometry table accessors: q = 0 cos, 1 sin, 2 dcos, 3 dl.

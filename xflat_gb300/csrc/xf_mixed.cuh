@@ -220,6 +220,16 @@ __device__ __forceinline__ F4 load_f(const float* __restrict__ b, int epad, int 
     return x;
 }
 
+// L1 prefetch of the four component rows of bin e: the load of a later
+// energy-loop iteration starts without holding registers.
+__device__ __forceinline__ void prefetch_f(const float* b, int epad, int e)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + e));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + epad + e));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + 2 * epad + e));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + 3 * epad + e));
+}
+
 __device__ __forceinline__ void store_f(float* __restrict__ b, int epad, int e, const F4& x)
 {
     b[e] = x.ar;
@@ -480,7 +490,9 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         KSum s[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) s[i] = KSum{0.f, 0.f};
+        const int pf = 32 * d.prefetch;
         for (int e = lane; e < epad; e += 32) {
+            if (pf && e + pf < epad) prefetch_f(in, epad, e + pf);
             const H3f h = bin_hf(g0, d.hvf[e], d.hvf[epad + e]);
             const F4 x = load_f(in, epad, e);
             const float lm = GEOM == 0 ? l0 : fmaxf(l0, l1);
@@ -561,7 +573,9 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         const float* in = p0 + (size_t)b * 4 * epad;
         const float* fvp = d.fvf + bi.p * epad;
         KSum s0{0.f, 0.f}, s2{0.f, 0.f}, s3{0.f, 0.f};
+        const int pf = 32 * d.prefetch;
         for (int e = lane; e < epad; e += 32) {
+            if (pf && e + pf < epad) prefetch_f(in, epad, e + pf);
             const H3f h = bin_hf(g3, d.hvf[e], d.hvf[epad + e]);
             const F4 x = load_f(in, epad, e);
             const KC k = warp_small_t(norm2(h) * (l1 * l1)) ? kcoef<2>(h, l1) : kcoef<5>(h, l1);
@@ -673,7 +687,12 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         const float* fvp = d.fvf + bi.p * epad;
         KSum s0{0.f, 0.f}, s2{0.f, 0.f}, s3{0.f, 0.f};
         float err = 0.f;
+        const int pf = 32 * d.prefetch;
         for (int e = lane; e < epad; e += 32) {
+            if (pf && e + pf < epad) {
+                prefetch_f(hi0 + base, epad, e + pf);
+                prefetch_f(lo0 + base, epad, e + pf);
+            }
             const float hv0 = d.hvf[e], hv1 = d.hvf[epad + e];
             const H3f h0 = bin_hf(g0, hv0, hv1), h1 = bin_hf(g1, hv0, hv1);
             const H3f h3 = bin_hf(g3, hv0, hv1), h4 = bin_hf(g4, hv0, hv1);
