@@ -1,0 +1,70 @@
+"""The whole config-0 run: MA 256 angle x 64 energy bins, 10 -> 300 km at
+tolerance 1e-9, seeded noise 1e-7 (xflat_gb300/configs/config0_ma.txt),
+about 1.1e7 stepper iterations, free-running under device control.
+
+- FP64 against the reference's own run of the same configuration
+  (tests/golden/c0_full_ref.npz, made by tests/golden/make_full_run.py with
+  the reference built from its sources): the same final radius, and P_ee(E)
+  of every nu_e beam within 1e-6 (absolute).  The accepted-step counts are
+  recorded, not compared: the last bits of the moment sums differ (another
+  summation order), and over 1e7 adaptive steps that may move a decision.
+- Mixed precision against FP64: P_ee(E) within 1e-5 and the per-beam survival
+  probabilities within 1e-5.
+
+It takes about 25 minutes on a GB300, so it runs only with XF_FULL_RUN=1;
+with XF_FULL_RUN_OUT=<dir> the final states and run statistics are saved
+there (full_run_{fp64,mixed}.npz)."""
+import os
+
+import numpy as np
+import pytest
+
+import xflat_gb300 as xg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CONFIG = os.path.join(ROOT, "xflat_gb300", "configs", "config0_ma.txt")
+REF = os.path.join(ROOT, "tests", "golden", "c0_full_ref.npz")
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("XF_FULL_RUN") != "1",
+                                 reason="the full 10 -> 300 km run takes ~25 GPU-minutes: set XF_FULL_RUN=1")]
+
+PEE_TOL_REF = 1e-6
+PEE_TOL_MIXED = 1e-5
+
+
+def pee(psi):
+    """P_ee(E) = |a(E)|^2 of the nu_e beams (particle index 0)."""
+    x = psi[0::4]
+    return x[:, 0] ** 2 + x[:, 1] ** 2
+
+
+def _run(prec):
+    text = open(CONFIG).read().replace("precision= fp64", "precision= " + prec)
+    sim = xg.Simulation(xg.Config.from_text(text))
+    out = sim.evolutionLoop(max_iters=-1, device_control=True)
+    psi = sim.get_state(0).copy()
+    surv = sim.survival().copy()
+    sim.close()
+    outdir = os.environ.get("XF_FULL_RUN_OUT")
+    if outdir:
+        os.makedirs(outdir, exist_ok=True)
+        np.savez(os.path.join(outdir, "full_run_%s.npz" % prec), psi=psi, survival=surv,
+                 iterations=out["iterations"], accepted=out["accepted"], r_end=out["r_end"],
+                 device_ms=out["device_ms"])
+    return out, psi, surv
+
+
+def test_config0_full_run():
+    o64, psi64, s64 = _run("fp64")
+    o32, psi32, s32 = _run("mixed")
+    for o in (o64, o32):
+        assert o["status"] == 0 and o["r_end"] == 300.0
+    d_mixed = np.max(np.abs(pee(psi32) - pee(psi64)))
+    assert d_mixed <= PEE_TOL_MIXED, d_mixed
+    assert np.max(np.abs(s32 - s64)) <= PEE_TOL_MIXED
+    if os.path.exists(REF):
+        ref = np.load(REF)
+        assert float(ref["r_end"]) == 300.0
+        d_ref = np.max(np.abs(pee(psi64) - ref["pee"]))
+        assert d_ref <= PEE_TOL_REF, d_ref
