@@ -253,7 +253,8 @@ def ours(args, rank, world, dist):
 
     # --- mixed precision on the same workload (FP32 rotations and compensated
     # FP32 state, FP64 reductions/control): same start state, same K steps
-    mixed = mixed_leg(xg, text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
+    mixed = variant_leg(xg, "mixed", text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
+    dfl = variant_leg(xg, "df", text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
     batched = batched_leg(xg, args.batch_steps) if args.batch_steps > 0 else None
 
     # --- end to end through the C ABI with host buffers: state H2D from pinned
@@ -328,7 +329,7 @@ def ours(args, rank, world, dist):
                                   "frac": hbm_achieved / hbm_peak if hbm_peak else None,
                                   "algorithmic_bytes_per_bin": PHASE_BYTES[dom]}},
         "phases_ms": {p: phase_ms[i] for i, p in enumerate("ABC")},
-        "variants": {"fp64": {"value": value, "unit": UNIT}, "mixed": mixed, "batched": batched},
+        "variants": {"fp64": {"value": value, "unit": UNIT}, "mixed": mixed, "df": dfl, "batched": batched},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": (state_bytes + e["h2d_bytes"]) /
                 max(1, e["iterations"]), "d2h_bytes_per_step": (state_bytes + e["d2h_bytes"]) /
@@ -351,19 +352,25 @@ def pee(psi):
     return x[:, 0] ** 2 + x[:, 1] ** 2
 
 
-def mixed_leg(xg, text, psi_start, r0, dr0, steps, bins, psi_fp64_end, surv_fp64, st64):
-    """Mixed-precision run of the same K steps from the same state; accuracy
-    against the FP64 run: max |dP_ee(E)| over every nu_e beam and max
+VARIANT_WORKLOAD = {
+    "mixed": "same as the FP64 line, precision= mixed (FP32 rotations and compensated FP32 state; "
+             "FP64 moment reduction, error estimate, control, renormalisation)",
+    "df": "same as the FP64 line, precision= df (every state, propagator, average and moment in double-float "
+          "FP32 pairs; FP64 block reduction and control)",
+}
+
+
+def variant_leg(xg, prec, text, psi_start, r0, dr0, steps, bins, psi_fp64_end, surv_fp64, st64):
+    """Run of the same K steps from the same state in another precision;
+    accuracy against the FP64 run: max |dP_ee(E)| over every nu_e beam and max
     per-beam survival-probability error (src/IO_f.cpp:341-351 quantity)."""
     import numpy as np
-    m = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= mixed")))
+    m = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= " + prec)))
     m.set_state(psi_start)
     out = m.evolutionLoop(max_iters=steps, device_control=True, iters_per_launch=min(16, steps), r0=r0, dr0=dr0)
     res = {"value": bins * out["iterations"] / (out["device_ms"] * 1e-3), "unit": UNIT,
            "ms_per_step": out["device_ms"] / max(1, out["iterations"]), "iterations": out["iterations"],
-           "accepted": out["accepted"], "accepted_fp64": st64["accepted"],
-           "workload": "same as the FP64 line, precision= mixed (FP32 rotations and compensated FP32 state; "
-                       "FP64 moment reduction, error estimate, control, renormalisation)"}
+           "accepted": out["accepted"], "accepted_fp64": st64["accepted"], "workload": VARIANT_WORKLOAD[prec]}
     if out["accepted"] == st64["accepted"]:
         res["max_dPee_vs_fp64"] = float(np.max(np.abs(pee(m.get_state(0)) - pee(psi_fp64_end))))
         res["max_dsurvival_vs_fp64"] = float(np.max(np.abs(m.survival() - surv_fp64)))

@@ -46,7 +46,7 @@ enum {
  * single-angle bulb model (src/Phy_SA.cpp), one beam per particle, Abins and
  * Pbins ignored. */
 enum { XF_GEOM_MA = 0, XF_GEOM_MAA = 1, XF_GEOM_SA = 2 };
-enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
+enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1, XF_PREC_DF = 2 };
 
 /* Run configuration.  Fields carry the reference's Util:: values in the same
  * internal units after the same parse-time conversions (src/Parser.cpp:40-123:
@@ -55,7 +55,7 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1 };
  * reference leaves them uninitialized). */
 typedef struct xf_config {
     int geometry;        /* XF_GEOM_*  (extension key "geometry= MA|MAA|SA") */
-    int precision;       /* XF_PREC_*  (extension key "precision= fp64|mixed") */
+    int precision;       /* XF_PREC_*  (extension key "precision= fp64|mixed|df"; df: MA and SA) */
     int abins, pbins, ebins, flvs;
     int has_matter;      /* hasMatter= */
     int dump_mode;       /* dumpMode= (bit 1 snapshot file, bit 2 probability file) */

@@ -1,0 +1,131 @@
+"""Double-float path (precision= df: every state, propagator, average and
+moment as a pair of FP32 numbers, about 48 significant bits; MA and SA)
+against the reference's own outputs and the FP64 path.
+
+Bars: the reference's accepted-step sequence replayed, every beam's
+polarization vector within 1e-10 relative of the reference's (the FP64
+parity bar), and the same for the FP64 path's own accepted steps;
+free-running windows take the FP64 path's accept/reject decisions; the step
+error within 1e-5
+relative of FP64's (it is the difference of two pair states, each exact to
+about 3.6e-15 of the state)."""
+import numpy as np
+import pytest
+
+import xflat_gb300 as xg
+from helpers import derive, golden, noise_state, pol_rel_err, replay_inputs
+
+pytestmark = pytest.mark.gpu
+
+POL_TOL = 1e-10
+
+
+def _df(text):
+    return text.replace("precision= fp64", "precision= df")
+
+
+def _pair(text, seed=1, amp=1e-7):
+    a = xg.Simulation(xg.Config.from_text(text))
+    b = xg.Simulation(xg.Config.from_text(_df(text)))
+    psi = noise_state(a.nbeams, a.ebins, seed, amp)
+    a.set_state(psi)
+    b.set_state(psi)
+    return a, b
+
+
+def pee(psi):
+    """P_ee(E) = |a(E)|^2 of the nu_e beams (particle index 0)."""
+    x = psi[0::4]
+    return x[:, 0] ** 2 + x[:, 1] ** 2
+
+
+@pytest.mark.parametrize("name", ["ma_small_r10", "ma_ragged_nh", "ma_small_r290", "ma_c0shape", "sa_r10", "sa_ragged"])
+def test_replay_reference_step_sequence(name):
+    g = golden(name)
+    sim = xg.Simulation(xg.Config.from_text(_df(g["config"])))
+    sim.set_state(noise_state(sim.nbeams, sim.ebins, g["meta"]["seed"], g["meta"]["noise_amp"]))
+    rb, dr = replay_inputs(g["config"], g["log"])
+    sim.replay(rb, dr)
+    err = pol_rel_err(sim.get_state(0), g["final"].reshape(sim.state_shape))
+    assert err <= POL_TOL, err
+
+
+@pytest.mark.parametrize("r,dr", [(10.0, 1.3e-8), (20.0, 1.2e-5), (50.0, 1.5e-4), (200.0, 5e-3), (40.0, 0.05)])
+def test_one_iteration_vs_fp64(r, dr):
+    """Includes a step with t = |h|^2 dl^2 above 1e-3 (the pair Horner series)."""
+    a, b = _pair(derive("config0_ma.txt", Abins=32, Ebins=64))
+    me64 = a.step(r, dr)
+    me2 = b.step(r, dr)
+    assert abs(me2 - me64) <= 1e-5 * me64, (me2, me64)
+    a.accept()
+    b.accept()
+    assert np.max(np.abs(b.get_state(0) - a.get_state(0))) <= 1e-13
+
+
+@pytest.mark.parametrize("r0,iters", [(10.0, 400), (50.0, 300)])
+def test_free_running_window_vs_fp64(r0, iters):
+    text = derive("config0_ma.txt", Abins=64, Ebins=64, R0=r0, dr="1e-6")
+    a, b = _pair(text)
+    oa = a.evolutionLoop(max_iters=iters, log_cap=1000)
+    ob = b.evolutionLoop(max_iters=iters, log_cap=1000)
+    assert (oa["iterations"], oa["accepted"]) == (ob["iterations"], ob["accepted"])
+    # the step error is the difference of two pair states (exact to about
+    # 3.6e-15 of the state, against a difference near 1e-9): dr follows FP64's
+    # to about 1e-6 relative per step, and the integrator's own truncation
+    # error (eps0 = 1e-9 per step) follows the step sequence
+    np.testing.assert_allclose(ob["log"][:, 2], oa["log"][:, 2], rtol=1e-4)
+    d = np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0))))
+    assert d <= 1e-8, d
+
+
+@pytest.mark.parametrize("r0,iters", [(10.0, 400), (50.0, 300)])
+def test_fp64_step_sequence_replayed(r0, iters):
+    """The FP64 path's accepted steps replayed in double-float: the arithmetic
+    alone, every polarization vector within the FP64 parity bar."""
+    text = derive("config0_ma.txt", Abins=64, Ebins=64, R0=r0, dr="1e-6")
+    a, b = _pair(text)
+    oa = a.evolutionLoop(max_iters=iters, log_cap=1000)
+    rb, dr = replay_inputs(text, oa["log"][:oa["accepted"]])
+    b.replay(rb, dr)
+    assert pol_rel_err(b.get_state(0), a.get_state(0)) <= POL_TOL
+
+
+def test_device_control_equals_host_loop():
+    text = _df(derive("config0_ma.txt", Abins=32, Ebins=64))
+    s1 = xg.Simulation(xg.Config.from_text(text))
+    s2 = xg.Simulation(xg.Config.from_text(text))
+    a = s1.evolutionLoop(max_iters=250, log_cap=1000)
+    b = s2.evolutionLoop(max_iters=250, log_cap=1000, device_control=True, iters_per_launch=16)
+    assert (a["iterations"], a["accepted"]) == (b["iterations"], b["accepted"])
+    np.testing.assert_array_equal(a["log"], b["log"])
+    assert np.array_equal(s1.get_state(0), s2.get_state(0))
+
+
+def test_config1_shape_window_vs_fp64():
+    """The 2048 x 4 x 512-bin workload: 20 device-controlled iterations from 50 km."""
+    text = derive("config1_ma.txt", R0=50, dr="1.5e-4")
+    a, b = _pair(text)
+    oa = a.evolutionLoop(max_iters=20, device_control=True)
+    ob = b.evolutionLoop(max_iters=20, device_control=True)
+    assert (oa["iterations"], oa["accepted"]) == (ob["iterations"], ob["accepted"])
+    assert abs(ob["last_max_err"] - oa["last_max_err"]) <= 1e-5 * oa["last_max_err"]
+    d = np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0))))
+    assert d <= 1e-11, d
+    # the candidate's per-beam survival sums from the pair state
+    assert np.max(np.abs(a.survival() - b.survival())) <= 1e-11
+
+
+def test_unitarity_without_renormalisation():
+    text = _df(derive("config0_ma.txt", Abins=32, Ebins=64))
+    s = xg.Simulation(xg.Config.from_text(text))
+    s.evolutionLoop(max_iters=2000, device_control=True)
+    psi = s.get_state(0)
+    n = psi[:, 0] ** 2 + psi[:, 1] ** 2 + psi[:, 2] ** 2 + psi[:, 3] ** 2
+    assert np.max(np.abs(n - 1.0)) <= 1e-12
+
+
+def test_unsupported_combinations():
+    with pytest.raises(xg.XflatError):
+        xg.Simulation(xg.Config.from_text(_df(derive("config3_maa.txt", Abins=8, Pbins=4, Ebins=16))))
+    with pytest.raises(xg.XflatError):
+        xg.Batch([xg.Config.from_text(_df(derive("config0_ma.txt", Abins=8, Ebins=16)))])

@@ -17,10 +17,15 @@ about 1.1e7 stepper iterations, free-running under device control.
   path perturb each step by about 5e5 times FP64's rounding; windows of a
   few hundred steps stay within 1e-5 (test_gpu_mixed.py), whole runs through
   the instability do not.
+- Double-float against FP64 at 300 km: P_ee(E) within 1e-5.  Its per-step
+  rounding is about 30 times FP64's (pairs of FP32 carry about 48 bits),
+  which the amplification above turns into a few 1e-6: measured on a GB300,
+  the same 11,161,528 iterations and accepted steps as FP64, max 8.9e-6
+  (median 4.6e-7), per-beam survival 2.1e-6.
 
 It takes about 25 minutes on a GB300, so it runs only with XF_FULL_RUN=1;
 with XF_FULL_RUN_OUT=<dir> the final states and run statistics are saved
-there (full_run_{fp64,mixed}.npz)."""
+there (full_run_{fp64,mixed,df}.npz)."""
 import os
 
 import numpy as np
@@ -86,3 +91,11 @@ def test_config0_full_run_mixed_vs_fp64():
     d_mixed = np.max(np.abs(pee(psi32) - pee(psi64)))
     assert d_mixed <= PEE_TOL_MIXED, d_mixed
     assert np.max(np.abs(s32 - s64)) <= PEE_TOL_MIXED
+
+
+def test_config0_full_run_df_vs_fp64():
+    _, psi64, s64 = _run("fp64")
+    _, psi2, s2 = _run("df")
+    d = np.max(np.abs(pee(psi2) - pee(psi64)))
+    assert d <= PEE_TOL_MIXED, d
+    assert np.max(np.abs(s2 - s64)) <= PEE_TOL_MIXED

@@ -22,11 +22,11 @@ import math
 import numpy as np
 
 from . import _abi
-from ._abi import (XF_EINVAL, XF_ENAN, XF_GEOM_MA, XF_GEOM_MAA, XF_GEOM_SA, XF_OK, XF_PREC_FP64, XF_PREC_MIXED, XfConfig,
+from ._abi import (XF_EINVAL, XF_ENAN, XF_GEOM_MA, XF_GEOM_MAA, XF_GEOM_SA, XF_OK, XF_PREC_DF, XF_PREC_FP64, XF_PREC_MIXED, XfConfig,
                    XfRunOpts, XfRunStats)
 
 __all__ = ["XflatError", "Parser", "Config", "Simulation", "Batch", "load", "XF_GEOM_MA", "XF_GEOM_MAA", "XF_GEOM_SA",
-           "XF_PREC_FP64", "XF_PREC_MIXED"]
+           "XF_PREC_DF", "XF_PREC_FP64", "XF_PREC_MIXED"]
 
 
 class XflatError(RuntimeError):

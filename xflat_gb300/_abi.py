@@ -10,7 +10,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libxflat_gb300.so")
 
 XF_OK, XF_EINVAL, XF_ECUDA, XF_ETIMEOUT, XF_ENAN, XF_EIO, XF_ENOMEM, XF_EUNSUPPORTED = range(8)
 XF_GEOM_MA, XF_GEOM_MAA, XF_GEOM_SA = 0, 1, 2
-XF_PREC_FP64, XF_PREC_MIXED = 0, 1
+XF_PREC_FP64, XF_PREC_MIXED, XF_PREC_DF = 0, 1, 2
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
 c_long_p = ctypes.POINTER(ctypes.c_long)

@@ -337,7 +337,8 @@ int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out)
     if (!cfgs || n <= 0 || !out) return XF_EINVAL;
     *out = nullptr;
     for (int i = 0; i < n; ++i)
-        if ((cfgs[i].geometry != XF_GEOM_MA && cfgs[i].geometry != XF_GEOM_SA) || cfgs[i].precision != cfgs[0].precision)
+        if ((cfgs[i].geometry != XF_GEOM_MA && cfgs[i].geometry != XF_GEOM_SA) || cfgs[i].precision != cfgs[0].precision ||
+            cfgs[i].precision == XF_PREC_DF)
             return XF_EUNSUPPORTED;
     xf_batch* b = new xf_batch();
     b->prec = cfgs[0].precision;

@@ -130,6 +130,7 @@ int parse_stream(std::istream& in, xf_config* c)
             ss >> s;
             if (s == "fp64" || s == "FP64") c->precision = XF_PREC_FP64;
             else if (s == "mixed" || s == "MIXED") c->precision = XF_PREC_MIXED;
+            else if (s == "df" || s == "DF") c->precision = XF_PREC_DF;
             else return XF_EINVAL;
         }
         else if (k == "seed=") { unsigned long long s = 0; ss >> s; c->seed = s; }

@@ -138,6 +138,8 @@ struct Dev {
     int renorm_every;     // mixed precision: renormalise psi0 every this many accepted steps
     int debug_psi3;       // phase C also stores U(h4, dl2) psi3 into psi3 (the reference's S10 result)
     int prefetch;         // mixed precision: L1 prefetch distance of the state rows, in energy-loop iterations
+    int df;               // double-float path (phase kernels of xf_df.cu on the compensated-pair state)
+    const float* hvf_lo;  // hvac - hvf rounded to FP32: (hvf, hvf_lo) is hvac as a double-float
 };
 
 // Geometry table accessors: q = 0 cos, 1 sin, 2 dcos, 3 dl.

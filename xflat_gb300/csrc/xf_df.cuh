@@ -1,0 +1,481 @@
+// Double-float per-phase kernel bodies (MA and SA geometry): the FP64 path's
+// stages, with every state, propagator, average and moment carried as a pair
+// of FP32 numbers (hi + lo, about 48 significant bits) and computed with FP32
+// error-free transformations instead of on the FP64 pipe, which runs at 1/64
+// of the FP32 rate on this GPU.
+//
+// The stages, buffers and reductions are those of xf_fp64.cuh: phase A forms
+// psi1 = U(h0, dl1) psi0 (stored halved) and psi3 = U(h0, dl0) psi0 with their
+// moments, phase B the average of S4/S5 into psi1 and psi4 = U(h3, dl1) psi0
+// (halved) with its moments, phase C the average of S10/S11 into the
+// candidate, the step error against psi1, the candidate's moments and the
+// step controller (src/Nmr.cpp:153-249, src/NBeam.cpp:360-393, 462-514,
+// 588-646, 690-736, 903-938).  Each propagator is U = q + (C - 1) - i S
+// sigma(h) (q = 1, or 1/2 for the halved forms): C - 1 = t c1(t) and
+// S = dl (1 + t s1(t)) with t = |h|^2 dl^2, whose leading constants are
+// pairs; when t <= 1e-3 in the whole warp (the bulb run's steps) the rest of
+// c1 and s1 is an FP32 tail below 3e-15 of C and S, otherwise the series is
+// a pair Horner up to t = 0.25 and FP64 sincos beyond.
+//
+// The per-beam Hamiltonian offsets are formed in FP64 (two operations per
+// offset, once per beam) and split into pairs; the vacuum term, energy
+// weights and path lengths come from pair tables.  Moments are accumulated
+// in pairs, scaled by kappa (add_moment_df), and reduced across blocks in
+// FP64.  psi0 and the candidate share the mixed path's compensated-pair
+// buffers; psi1 and psi3 are pairs stored in the FP64 path's buffers
+// ([nbeams][4][epad] hi, then lo).
+#pragma once
+#include "xf_mixed.cuh"
+
+namespace xf {
+namespace dfp {
+
+using namespace detail;
+using mixed::DF;
+using mixed::df_add;
+using mixed::df_mul;
+using mixed::df_neg;
+using mixed::df_sub;
+using mixed::df_value;
+using mixed::fast_two_sum;
+using mixed::two_prod;
+using mixed::two_sum;
+
+struct DF4 {
+    DF ar, ai, br, bi;
+};
+
+__device__ __forceinline__ DF4 load_df(const float* __restrict__ hi, const float* __restrict__ lo, int epad, int e)
+{
+    DF4 x;
+    x.ar = DF{hi[e], lo[e]};
+    x.ai = DF{hi[epad + e], lo[epad + e]};
+    x.br = DF{hi[2 * epad + e], lo[2 * epad + e]};
+    x.bi = DF{hi[3 * epad + e], lo[3 * epad + e]};
+    return x;
+}
+
+__device__ __forceinline__ void store_df(float* __restrict__ hi, float* __restrict__ lo, int epad, int e, const DF4& x)
+{
+    hi[e] = x.ar.h;
+    lo[e] = x.ar.l;
+    hi[epad + e] = x.ai.h;
+    lo[epad + e] = x.ai.l;
+    hi[2 * epad + e] = x.br.h;
+    lo[2 * epad + e] = x.br.l;
+    hi[3 * epad + e] = x.bi.h;
+    lo[3 * epad + e] = x.bi.l;
+}
+
+__device__ __forceinline__ DF dscale(float s, const DF& a) { return DF{s * a.h, s * a.l}; }  // s a power of two
+
+// a0 b0 + a1 b1 (the lo*lo products, 2^-48 of the terms, are dropped).
+__device__ __forceinline__ DF dot2(const DF& a0, const DF& b0, const DF& a1, const DF& b1)
+{
+    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h);
+    const DF s = two_sum(p.h, q.h);
+    const float cross = fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, fmaf(a1.h, b1.l, a1.l * b1.h)));
+    return fast_two_sum(s.h, s.l + ((p.l + q.l) + cross));
+}
+
+// a0 b0 + a1 b1 + a2 b2.
+__device__ __forceinline__ DF dot3(const DF& a0, const DF& b0, const DF& a1, const DF& b1, const DF& a2, const DF& b2)
+{
+    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h), r = two_prod(a2.h, b2.h);
+    const DF s = two_sum(p.h, q.h);
+    const DF u = two_sum(s.h, r.h);
+    const float cross = fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, fmaf(a1.h, b1.l, fmaf(a1.l, b1.h, fmaf(a2.h, b2.l, a2.l * b2.h)))));
+    return fast_two_sum(u.h, (s.l + u.l) + ((p.l + q.l + r.l) + cross));
+}
+
+__device__ __forceinline__ DF dsplit(double x)
+{
+    const float h = (float)x;
+    return DF{h, (float)(x - (double)h)};
+}
+
+// Propagator coefficients: U = q + cm - i S sigma(h), cm = q (C - 1).
+struct DK {
+    DF cm, S;
+};
+
+// Per-beam constants of a propagator: h01i^2 and dl^2 as pairs, and dl.
+struct DBeam {
+    DF h01i, h01i2, dl, dl2;
+};
+
+__device__ __forceinline__ DBeam dbeam(const DF& h01i, const DF& dl)
+{
+    DBeam b;
+    b.h01i = h01i;
+    b.h01i2 = df_mul(h01i, h01i);
+    b.dl = dl;
+    b.dl2 = df_mul(dl, dl);
+    return b;
+}
+
+// c1 = (cos(sqrt t) - 1)/t and s1 = (sin(sqrt t)/sqrt t - 1)/t: the Taylor
+// coefficients from k = 1 on (c: (-1)^k / (2k)!, s: (-1)^k / (2k+1)!), each
+// as a pair.
+struct DConst {
+    float h, l;
+};
+#define XF_DFC(v) DConst{(float)(v), (float)((v) - (double)(float)(v))}
+__constant__ DConst kDC[7] = {XF_DFC(-1.0 / 2.0),      XF_DFC(1.0 / 24.0),        XF_DFC(-1.0 / 720.0),
+                              XF_DFC(1.0 / 40320.0),   XF_DFC(-1.0 / 3628800.0),  XF_DFC(1.0 / 479001600.0),
+                              XF_DFC(-1.0 / 87178291200.0)};
+__constant__ DConst kDS[7] = {XF_DFC(-1.0 / 6.0),         XF_DFC(1.0 / 120.0),          XF_DFC(-1.0 / 5040.0),
+                              XF_DFC(1.0 / 362880.0),     XF_DFC(-1.0 / 39916800.0),    XF_DFC(1.0 / 6227020800.0),
+                              XF_DFC(-1.0 / 1307674368000.0)};
+#undef XF_DFC
+
+__device__ __forceinline__ DF dconst(const DConst& c) { return DF{c.h, c.l}; }
+
+// Coefficients of U over dl for the bin Hamiltonian (h00, h01r, beam h01i).
+// Must be called by all 32 lanes of the warp (warp-uniform series choice).
+template <int Q2>
+__device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DBeam& bm)
+{
+    constexpr float q = Q2 ? 0.5f : 1.f;
+    const DF lam2 = df_add(dot2(h00, h00, h01r, h01r), bm.h01i2);
+    const DF t = df_mul(lam2, bm.dl2);
+    DF c1, s1;
+    bool direct = false;
+    DK k;
+    if (__all_sync(kFull, t.h <= 1e-3f)) {
+        // tails t (1/24 - t/720) and t (1/120 - t/5040) in FP32: below 4.2e-5
+        // and 8.4e-6, rounded to 2^-24 of that; the next terms, t^3/40320 and
+        // t^3/362880, are below 2.5e-14 and 2.8e-15 of c1 and s1, and enter C
+        // and S times t
+        const float th = t.h;
+        c1 = fast_two_sum(-0.5f, th * fmaf(th, -1.f / 720.f, 1.f / 24.f));
+        s1 = df_add(dconst(kDS[0]), DF{th * fmaf(th, -1.f / 5040.f, 1.f / 120.f), 0.f});
+    } else if (t.h <= 0.25f) {
+        // pair Horner to degree 7 in t (truncation below 1e-18 at t = 0.25)
+        c1 = dconst(kDC[6]);
+        s1 = dconst(kDS[6]);
+#pragma unroll
+        for (int i = 5; i >= 0; --i) {
+            c1 = df_add(dconst(kDC[i]), df_mul(c1, t));
+            s1 = df_add(dconst(kDS[i]), df_mul(s1, t));
+        }
+    } else {
+        const double lam = sqrt(df_value(lam2));
+        const double dl = df_value(bm.dl);
+        double sn, cs;
+        sincos(lam * dl, &sn, &cs);
+        k.cm = dsplit(q * (cs - 1.0));
+        k.S = dsplit(q * (sn / lam));
+        direct = true;
+    }
+    if (!direct) {
+        k.cm = dscale(q, df_mul(t, c1));
+        k.S = dscale(q, df_add(bm.dl, df_mul(bm.dl, df_mul(t, s1))));
+    }
+    return k;
+}
+
+// w = -i sigma(h) x (the form of su2_w in xf_fp64.cuh).
+__device__ __forceinline__ DF4 dsig_w(const DF& h00, const DF& h01r, const DF& h01i, const DF4& x)
+{
+    DF4 w;
+    w.ar = dot3(h00, x.ai, h01i, x.br, h01r, x.bi);
+    w.ai = dot3(df_neg(h00), x.ar, h01i, x.bi, df_neg(h01r), x.br);
+    w.br = dot3(df_neg(h01i), x.ar, h01r, x.ai, df_neg(h00), x.bi);
+    w.bi = dot3(df_neg(h01i), x.ai, df_neg(h01r), x.ar, h00, x.br);
+    return w;
+}
+
+// y = U x = q x + cm x + S w.
+__device__ __forceinline__ DF4 dapply(float q, const DK& k, const DF4& x, const DF4& w)
+{
+    DF4 y;
+    y.ar = df_add(dscale(q, x.ar), dot2(k.cm, x.ar, k.S, w.ar));
+    y.ai = df_add(dscale(q, x.ai), dot2(k.cm, x.ai, k.S, w.ai));
+    y.br = df_add(dscale(q, x.br), dot2(k.cm, x.br, k.S, w.br));
+    y.bi = df_add(dscale(q, x.bi), dot2(k.cm, x.bi, k.S, w.bi));
+    return y;
+}
+
+__device__ __forceinline__ DF4 dadd4(const DF4& a, const DF4& b)
+{
+    DF4 c;
+    c.ar = df_add(a.ar, b.ar);
+    c.ai = df_add(a.ai, b.ai);
+    c.br = df_add(a.br, b.br);
+    c.bi = df_add(a.bi, b.bi);
+    return c;
+}
+
+// Accumulates fv * rho(x) (acc_rho of xf_fp64.cuh: component 0 without the 1/2).
+__device__ __forceinline__ void dacc_rho(const DF4& x, const DF& fv, DF& s0, DF& s2, DF& s3)
+{
+    const DF d0 = df_sub(dot2(x.ar, x.ar, x.ai, x.ai), dot2(x.br, x.br, x.bi, x.bi));
+    const DF d2 = dot2(x.ar, x.br, x.ai, x.bi);
+    const DF d3 = dot2(x.ai, x.br, df_neg(x.ar), x.bi);
+    s0 = df_add(s0, df_mul(d0, fv));
+    s2 = df_add(s2, df_mul(d2, fv));
+    s3 = df_add(s3, df_mul(d3, fv));
+}
+
+__device__ __forceinline__ DF shfl_df(const DF& v, int src)
+{
+    return DF{__shfl_sync(kFull, v.h, src), __shfl_sync(kFull, v.l, src)};
+}
+
+__device__ __forceinline__ DF hv_df(const Dev& d, int k, int e)
+{
+    return DF{d.hvf[k * d.epad + e], d.hvf_lo[k * d.epad + e]};
+}
+
+__device__ __forceinline__ DF fv_df(const Dev& d, int p, int e)
+{
+    return DF{d.fvf[p * d.epad + e], d.fvf_lo[p * d.epad + e]};
+}
+
+// psi1 / psi3 pair buffers inside the FP64 path's double buffers.
+__device__ __forceinline__ float* pair_hi(double* buf) { return reinterpret_cast<float*>(buf); }
+__device__ __forceinline__ size_t pair_span(const Dev& d) { return (size_t)d.nbeams * 4 * d.epad; }
+
+// ------------------------------------------------------------------ phase A
+
+template <int GEOM>
+__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt)
+{
+    static_assert(GEOM == 0, "the double-float path covers the MA and SA geometries");
+    constexpr int K = NK<GEOM>::K;
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    const float* __restrict__ h0 = ctl->m0hi;
+    const float* __restrict__ l0 = ctl->m0lo;
+    float* p1h = pair_hi(d.psi1);
+    float* p3h = pair_hi(d.psi3);
+    const size_t span = pair_span(d);
+    const double hm = ctl->hm[0];
+    const int lane = threadIdx.x & 31;
+    const int gw = first + (threadIdx.x >> 5), tw = stride;
+    const int epad = d.epad;
+    DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
+    const int myv = lane >> 2;
+    const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
+    for (int b = gw; b < d.nbeams; b += tw) {
+        const BeamIdx bi = decode_beam(d, b);
+        if (stage) stage_beam(d, ctl, stage, b, lane, nullptr, ctl->m0hi, ctl->m0lo);
+        // lane-parallel set-up: lanes 0-2 the offsets of H0 (FP64, split), lane 3 dl0
+        DF sv{0.f, 0.f};
+        if (lane < 3) sv = dsplit(beam_offset_k<GEOM>(d, ctl->J0, 0, hm, bi, lane));
+        else if (lane == 3) sv = mixed::dfg(d, 3, 0, bi.ang);
+        const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2), dl0 = shfl_df(sv, 3);
+        const DBeam bm = dbeam(g01i, dl0);
+        const size_t base = (size_t)b * 4 * epad;
+        DF v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = DF{0.f, 0.f};
+        for (int e = lane; e < epad; e += 32) {
+            const DF a00 = df_add(hv_df(d, 0, e), g00), a01 = df_add(hv_df(d, 1, e), g01r);
+            const DF4 x = load_df(h0 + base, l0 + base, epad, e);
+            const DK k0 = dcoeffs<0>(a00, a01, bm);
+            // MA: dl1 = 2 dl0, so the halved U(dl1) has C1/2 - 1/2 = C0^2 - 1 =
+            // cm0 (2 + cm0) and S1/2 = C0 S0 = S0 + cm0 S0
+            DK k1;
+            k1.cm = df_mul(k0.cm, df_add(DF{2.f, 0.f}, k0.cm));
+            k1.S = df_add(k0.S, df_mul(k0.cm, k0.S));
+            const DF4 w = dsig_w(a00, a01, g01i, x);
+            const DF4 y1 = dapply(.5f, k1, x, w);
+            const DF4 y3 = dapply(1.f, k0, x, w);
+            store_df(p1h + base, p1h + span + base, epad, e, y1);
+            store_df(p3h + base, p3h + span + base, epad, e, y3);
+            const DF f = fv_df(d, bi.p, e);
+            dacc_rho(y1, f, v[0], v[1], v[2]);
+            dacc_rho(y3, f, v[3], v[4], v[5]);
+        }
+        // psi1 was accumulated halved: its sums are a quarter (exactly) of psi1's
+        v[0] = dscale(2.f, v[0]);
+        v[1] = dscale(4.f, v[1]);
+        v[2] = dscale(4.f, v[2]);
+        v[3] = dscale(.5f, v[3]);
+        mixed::df_reduce_scatter<8>(v, lane);
+        if (myv < 3) mixed::add_moment_df<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 3, acc);
+        else if (myv < 6) mixed::add_moment_df<GEOM>(d, v[0], comp_of(myv - 3), 1, bi, lane & 3, acc);
+    }
+    if (!group_reduce_split<K>(rt, 4, 6, df_value(acc), 0., false, s_warp, s_out)) return;
+    stage_done(ctl);
+    if (threadIdx.x < kNJ) {
+        ctl->JA1[threadIdx.x] = 0.;
+        ctl->JA3[threadIdx.x] = 0.;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < 6 * K) {
+        const int v = threadIdx.x / K, k = threadIdx.x % K;
+        double* J = v < 3 ? ctl->JA1 : ctl->JA3;
+        J[k * 4 + comp_of(v % 3)] = s_out[threadIdx.x] / d.kappa;
+    }
+}
+
+// ------------------------------------------------------------------ phase B
+
+template <int GEOM>
+__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt)
+{
+    static_assert(GEOM == 0, "the double-float path covers the MA and SA geometries");
+    constexpr int K = NK<GEOM>::K;
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    const float* __restrict__ h0 = ctl->m0hi;
+    const float* __restrict__ l0 = ctl->m0lo;
+    float* h4 = ctl->m4hi;
+    float* l4 = ctl->m4lo;
+    float* p1h = pair_hi(d.psi1);
+    const size_t span = pair_span(d);
+    const double hm_rdr = ctl->hm[2], hm_rdr2 = ctl->hm[1];
+    const int lane = threadIdx.x & 31;
+    const int gw = first + (threadIdx.x >> 5), tw = stride;
+    const int epad = d.epad;
+    DF acc{0.f, 0.f};
+    const int myv = lane >> 3;
+    for (int b = gw; b < d.nbeams; b += tw) {
+        const BeamIdx bi = decode_beam(d, b);
+        // lane-parallel set-up: lanes 0-2 the offsets of H1, 3-5 those of H3, lane 6 dl1
+        DF sv{0.f, 0.f};
+        if (lane < 3) sv = dsplit(beam_offset_k<GEOM>(d, ctl->JA1, 2, hm_rdr, bi, lane));
+        else if (lane < 6) sv = dsplit(beam_offset_k<GEOM>(d, ctl->JA3, 1, hm_rdr2, bi, lane - 3));
+        else if (lane == 6) sv = mixed::dfg(d, 3, 1, bi.ang);
+        const DF g100 = shfl_df(sv, 0), g101r = shfl_df(sv, 1), g101i = shfl_df(sv, 2);
+        const DF g300 = shfl_df(sv, 3), g301r = shfl_df(sv, 4), g301i = shfl_df(sv, 5);
+        const DF dl1 = shfl_df(sv, 6);
+        const DBeam ba = dbeam(g101i, dl1), bb = dbeam(g301i, dl1);
+        const size_t base = (size_t)b * 4 * epad;
+        DF v[4] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
+        for (int e = lane; e < epad; e += 32) {
+            const DF hv0 = hv_df(d, 0, e), hv1 = hv_df(d, 1, e);
+            const DF4 x = load_df(h0 + base, l0 + base, epad, e);
+            // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
+            const DF a00 = df_add(hv0, g100), a01 = df_add(hv1, g101r);
+            const DK ka = dcoeffs<1>(a00, a01, ba);
+            const DF4 ya = dapply(.5f, ka, x, dsig_w(a00, a01, g101i, x));
+            const DF4 p1 = load_df(p1h + base, p1h + span + base, epad, e);
+            store_df(p1h + base, p1h + span + base, epad, e, dadd4(ya, p1));
+            // S8, stored halved for the average of S10/S11
+            const DF b00 = df_add(hv0, g300), b01 = df_add(hv1, g301r);
+            const DK kb = dcoeffs<1>(b00, b01, bb);
+            const DF4 y4 = dapply(.5f, kb, x, dsig_w(b00, b01, g301i, x));
+            store_df(h4 + base, l4 + base, epad, e, y4);
+            dacc_rho(y4, fv_df(d, bi.p, e), v[0], v[1], v[2]);
+        }
+        // psi4 was accumulated halved: its sums are a quarter (exactly) of psi4's
+        v[0] = dscale(2.f, v[0]);
+        v[1] = dscale(4.f, v[1]);
+        v[2] = dscale(4.f, v[2]);
+        mixed::df_reduce_scatter<4>(v, lane);
+        if (myv < 3) mixed::add_moment_df<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 7, acc);
+    }
+    if (!group_reduce_split<K>(rt, 8, 3, df_value(acc), 0., false, s_warp, s_out)) return;
+    if (threadIdx.x < kNJ) ctl->JB4[threadIdx.x] = 0.;
+    __syncthreads();
+    if ((int)threadIdx.x < 3 * K) {
+        const int v = threadIdx.x / K, k = threadIdx.x % K;
+        ctl->JB4[k * 4 + comp_of(v)] = s_out[threadIdx.x] / d.kappa;
+    }
+}
+
+// ------------------------------------------------------------------ phase C
+
+template <int GEOM>
+__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt)
+{
+    static_assert(GEOM == 0, "the double-float path covers the MA and SA geometries");
+    constexpr int K = NK<GEOM>::K;
+    Ctl* ctl = d.ctl;
+    if (ctl->done) return;
+    __shared__ double s_warp[8 * 32];
+    __shared__ double s_out[32];
+    float* h4 = ctl->m4hi;
+    float* l4 = ctl->m4lo;
+    double* __restrict__ S4 = ctl->S4;
+    float2* __restrict__ S4f = ctl->S4f;
+    const float* p1h = pair_hi(d.psi1);
+    const float* p3h = pair_hi(d.psi3);
+    const size_t span = pair_span(d);
+    const double hm_rdr = ctl->hm[2];
+    const int lane = threadIdx.x & 31;
+    const int gw = first + (threadIdx.x >> 5), tw = stride;
+    const int epad = d.epad;
+    DF acc{0.f, 0.f};
+    float mx = -1.f;
+    const int myv = lane >> 3;  // 0: error, 1..3: density components 0, 2, 3
+    for (int b = gw; b < d.nbeams; b += tw) {
+        const BeamIdx bi = decode_beam(d, b);
+        // lane-parallel set-up: lanes 0-2 the offsets of H4, lane 3 dl2
+        DF sv{0.f, 0.f};
+        if (lane < 3) sv = dsplit(beam_offset_k<GEOM>(d, ctl->JB4, 2, hm_rdr, bi, lane));
+        else if (lane == 3) sv = mixed::dfg(d, 3, 2, bi.ang);
+        const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2), dl2 = shfl_df(sv, 3);
+        const DBeam bm = dbeam(g01i, dl2);
+        const size_t base = (size_t)b * 4 * epad;
+        DF v[4] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
+        float err = 0.f;
+        for (int e = lane; e < epad; e += 32) {
+            const DF a00 = df_add(hv_df(d, 0, e), g00), a01 = df_add(hv_df(d, 1, e), g01r);
+            const DF4 x3 = load_df(p3h + base, p3h + span + base, epad, e);
+            // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
+            const DK k = dcoeffs<1>(a00, a01, bm);
+            const DF4 y3 = dapply(.5f, k, x3, dsig_w(a00, a01, g01i, x3));
+            const DF4 c = dadd4(y3, load_df(h4 + base, l4 + base, epad, e));
+            store_df(h4 + base, l4 + base, epad, e, c);
+            // calcErrHvv against psi1: the difference of two pairs is exact to
+            // 2^-48 of the state, far below the error's own size
+            const DF4 r1 = load_df(p1h + base, p1h + span + base, epad, e);
+            const float e0 = df_sub(c.ar, r1.ar).h, e1 = df_sub(c.ai, r1.ai).h;
+            const float e2 = df_sub(c.br, r1.br).h, e3 = df_sub(c.bi, r1.bi).h;
+            const DF f = fv_df(d, bi.p, e);
+            err = fmaf((e0 * e0 + e1 * e1) + (e2 * e2 + e3 * e3), f.h, err);
+            dacc_rho(c, f, v[1], v[2], v[3]);
+        }
+        v[0] = DF{err, 0.f};
+        v[1] = dscale(.5f, v[1]);
+        mixed::df_reduce_scatter<4>(v, lane);
+        if (myv == 0) {
+            mx = fmaxf(mx, v[0].h + v[0].l);
+            if ((lane & 7) == 0) {
+                S4[(size_t)b * 4 + 1] = 0.;
+                S4f[(size_t)b * 4 + 1] = make_float2(0.f, 0.f);
+            }
+        } else {
+            const int comp = comp_of(myv - 1);
+            mixed::add_moment_df<GEOM>(d, v[0], comp, 2, bi, lane & 7, acc);
+            // per-beam moments of the candidate (the reference's hSumMat of psi4)
+            if ((lane & 7) == 0) {
+                S4[(size_t)b * 4 + comp] = df_value(v[0]);
+                S4f[(size_t)b * 4 + comp] = make_float2(v[0].h, v[0].l);
+            }
+        }
+    }
+    const double accs = __shfl_down_sync(kFull, df_value(acc), 8);
+    if (!group_reduce_split<K>(rt, 8, 3, accs, (double)mx, true, s_warp, s_out)) return;
+    if (threadIdx.x < kNJ) ctl->JC[threadIdx.x] = 0.;
+    __syncthreads();
+    if ((int)threadIdx.x < 3 * K) {
+        const int v = threadIdx.x / K, k = threadIdx.x % K;
+        ctl->JC[k * 4 + comp_of(v)] = s_out[threadIdx.x] / d.kappa;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double me = sqrt(s_out[31]);
+        ctl->max_err = me;
+        if (d.device_control && step_control(d, ctl, me)) {
+            float* t = ctl->m0hi;
+            ctl->m0hi = ctl->m4hi;
+            ctl->m4hi = t;
+            t = ctl->m0lo;
+            ctl->m0lo = ctl->m4lo;
+            ctl->m4lo = t;
+        }
+    }
+}
+
+}  // namespace dfp
+}  // namespace xf

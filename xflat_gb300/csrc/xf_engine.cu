@@ -45,7 +45,14 @@ int check_config(const xf_config& c, std::string& why)
         why = "geometry must be MA, MAA or SA";
         return XF_EINVAL;
     }
-    if (c.precision != XF_PREC_FP64 && c.precision != XF_PREC_MIXED) { why = "precision must be fp64 or mixed"; return XF_EINVAL; }
+    if (c.precision != XF_PREC_FP64 && c.precision != XF_PREC_MIXED && c.precision != XF_PREC_DF) {
+        why = "precision must be fp64, mixed or df";
+        return XF_EINVAL;
+    }
+    if (c.precision == XF_PREC_DF && c.geometry == XF_GEOM_MAA) {
+        why = "the double-float path covers the MA and SA geometries";
+        return XF_EUNSUPPORTED;
+    }
     if (c.flvs != 2) { why = "only two flavors are supported (Flvs= 2), as by the MA/MAA modules"; return XF_EUNSUPPORTED; }
     if ((c.geometry != XF_GEOM_SA && c.abins <= 0) || c.ebins <= 0) { why = "Abins and Ebins must be positive"; return XF_EINVAL; }
     if (c.geometry == XF_GEOM_MAA && c.pbins <= 0) { why = "Pbins must be positive for MAA"; return XF_EINVAL; }
@@ -98,6 +105,7 @@ int xf_handle::init(const xf_config& c)
     epad = (ne + 31) / 32 * 32;
     nbeams = A * P * 4;
     shape = xf::default_shape(nbeams, epad, cfg.precision == XF_PREC_MIXED);
+    if (cfg.precision == XF_PREC_DF) renorm_every = 0;  // pair arithmetic keeps |a|^2 + |b|^2 = 1 to 2^-48
     XF_CUDA(this, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     for (int i = 0; i < 7; ++i) XF_CUDA(this, cudaEventCreate(&ev[i]));
 
@@ -159,7 +167,7 @@ int xf_handle::init(const xf_config& c)
     dev.cosphi = d_cosphi;
     dev.sinphi = d_sinphi;
     dev.geo = d_geo;
-    dev.geof = cfg.precision == XF_PREC_MIXED ? d_geof : nullptr;  // the FP64 path reads only geo
+    dev.geof = cfg.precision != XF_PREC_FP64 ? d_geof : nullptr;  // the FP64 path reads only geo
     dev.cosphif = d_phif;
     dev.sinphif = d_phif + 2 * cphi.size();
     dev.partials = d_partials;
@@ -187,9 +195,17 @@ int xf_handle::init(const xf_config& c)
     dev.nb0 = cfg.nb0;
     dev.hNS = cfg.hNS;
 
-    if (cfg.precision == XF_PREC_MIXED) {
+    if (cfg.precision != XF_PREC_FP64) {
         mixed = xf::mixed_create(this);
         if (!mixed) return err.empty() ? fail(XF_ENOMEM, "mixed-precision state allocation failed") : XF_ENOMEM;
+        if (cfg.precision == XF_PREC_DF) {
+            // psi1 and psi3 as compensated pairs, hi then lo, in FP64-sized buffers
+            const size_t nst = (size_t)nbeams * 4 * epad;
+            if ((rc = dalloc(this, &d_psi[1], nst)) || (rc = dalloc(this, &d_psi[2], nst))) return rc;
+            dev.psi1 = d_psi[1];
+            dev.psi3 = d_psi[2];
+            dev.df = 1;
+        }
     } else {
         const size_t nst = (size_t)nbeams * 4 * epad;
         for (int i = 0; i < 4; ++i)
@@ -465,7 +481,7 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
     XF_CUDA(this, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int i = 0; i < k; ++i) {
         xf::launch_geometry(d, st);
-        if (mixed) {
+        if (mixed && !dev.df) {
             // after a flagged accepted step: renormalise psi0, refresh its exact
             // sums and its moments at stage point 0 of the new radius
             xf::mixed_launch_renorm(d, 1, st);
@@ -701,7 +717,7 @@ int xf_set_option(xf_handle* h, const char* name, double value)
         const int b = (int)value;
         const int cap = std::max(xf::max_phase_blocks(h->nbeams, 256), 152 * 4);
         if (b < 0 || b > cap) return h->fail(XF_EINVAL, "blocks out of range");
-        const xf::Shape def = xf::default_shape(h->nbeams, h->epad, h->mixed != nullptr);
+        const xf::Shape def = xf::default_shape(h->nbeams, h->epad, h->mixed != nullptr && !h->dev.df);
         h->shape.blocks = b ? b : def.blocks;
         h->shape.blocks_ab = b ? b : def.blocks_ab;
     } else {

@@ -122,6 +122,7 @@ struct Mixed {
     float* fvf = nullptr;
     float* fvf_lo = nullptr;
     float* hvf = nullptr;
+    float* hvf_lo = nullptr;
     double* S[2] = {nullptr, nullptr};
     float2* Sf[2] = {nullptr, nullptr};
 };
@@ -144,23 +145,28 @@ Mixed* mixed_create(xf_handle* h)
         ok = ok && cudaMalloc(&m->Sf[i], 4 * (size_t)h->nbeams * sizeof(float2)) == cudaSuccess &&
              cudaMemset(m->Sf[i], 0, 4 * (size_t)h->nbeams * sizeof(float2)) == cudaSuccess;
     }
-    std::vector<float> fvf(4 * (size_t)h->epad, 0.f), fvf_lo(4 * (size_t)h->epad, 0.f), hvf(2 * (size_t)h->epad, 0.f);
+    std::vector<float> fvf(4 * (size_t)h->epad, 0.f), fvf_lo(4 * (size_t)h->epad, 0.f), hvf(2 * (size_t)h->epad, 0.f),
+        hvf_lo(2 * (size_t)h->epad, 0.f);
     for (int p = 0; p < 4; ++p)
         for (int e = 0; e < h->ne; ++e) {
             const double f = h->tab.fv[(size_t)p * h->ne + e];
             fvf[(size_t)p * h->epad + e] = (float)f;
             fvf_lo[(size_t)p * h->epad + e] = (float)(f - (double)(float)f);
         }
-    for (int e = 0; e < h->ne; ++e) {
-        hvf[e] = (float)h->tab.hvac[2 * (size_t)e];
-        hvf[h->epad + e] = (float)h->tab.hvac[2 * (size_t)e + 1];
-    }
+    for (int e = 0; e < h->ne; ++e)
+        for (int k = 0; k < 2; ++k) {
+            const double v = h->tab.hvac[2 * (size_t)e + k];
+            hvf[k * h->epad + e] = (float)v;
+            hvf_lo[k * h->epad + e] = (float)(v - (double)(float)v);
+        }
     ok = ok && cudaMalloc(&m->fvf, fvf.size() * sizeof(float)) == cudaSuccess &&
          cudaMemcpy(m->fvf, fvf.data(), fvf.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMalloc(&m->fvf_lo, fvf_lo.size() * sizeof(float)) == cudaSuccess &&
          cudaMemcpy(m->fvf_lo, fvf_lo.data(), fvf_lo.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMalloc(&m->hvf, hvf.size() * sizeof(float)) == cudaSuccess &&
          cudaMemcpy(m->hvf, hvf.data(), hvf.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMalloc(&m->hvf_lo, hvf_lo.size() * sizeof(float)) == cudaSuccess &&
+         cudaMemcpy(m->hvf_lo, hvf_lo.data(), hvf_lo.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     if (!ok) {
         h->fail(XF_ENOMEM, "mixed-precision state allocation failed");
         mixed_destroy(m);
@@ -169,6 +175,7 @@ Mixed* mixed_create(xf_handle* h)
     h->dev.fvf = m->fvf;
     h->dev.fvf_lo = m->fvf_lo;
     h->dev.hvf = m->hvf;
+    h->dev.hvf_lo = m->hvf_lo;
     h->h_ctl->m0hi = m->hi[0];
     h->h_ctl->m0lo = m->lo[0];
     h->h_ctl->m4hi = m->hi[1];
@@ -197,6 +204,7 @@ void mixed_destroy(Mixed* m)
     if (m->fvf) cudaFree(m->fvf);
     if (m->fvf_lo) cudaFree(m->fvf_lo);
     if (m->hvf) cudaFree(m->hvf);
+    if (m->hvf_lo) cudaFree(m->hvf_lo);
     delete m;
 }
 
@@ -240,6 +248,10 @@ int mixed_get_state(xf_handle* h, Mixed* m, int which, double* psi)
 
 void mixed_launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
 {
+    if (d.df) {
+        df_launch_phase(phase, d, sh, st);
+        return;
+    }
     const int ab = sh.blocks_ab > 0 ? sh.blocks_ab : sh.blocks;
     if (d.geom == 0) {
         if (phase == PH_A) launch_pdl(k_mixA<0>, ab, sh.threads, st, d);

@@ -17,6 +17,8 @@ void mixed_destroy(Mixed* m);
 int mixed_set_state(xf_handle* h, Mixed* m, const double* psi);
 int mixed_get_state(xf_handle* h, Mixed* m, int which, double* psi);
 void mixed_launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st);
+// Phase kernels of the double-float path (xf_df.cu), on the same state buffers.
+void df_launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st);
 void mixed_launch_accept(const Dev& d, cudaStream_t st);
 // Renormalises psi0 and recomputes its exact FP64 energy sums; with
 // `conditional` only when the step controller flagged it.
