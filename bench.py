@@ -251,8 +251,9 @@ def ours(args, rank, world, dist):
     psi_fp64_end = sim.get_state(0).copy()
     surv_fp64 = sim.survival()
 
-    # --- mixed precision on the same workload (FP32 rotations and compensated
-    # FP32 state, FP64 reductions/control): same start state, same K steps
+    # --- mixed precision (FP32 rotations and compensated FP32 state, FP64
+    # reductions/control) and double-float (every operation in FP32 pairs) on
+    # the same workload: same start state, same K steps
     mixed = variant_leg(xg, "mixed", text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
     dfl = variant_leg(xg, "df", text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
     batched = batched_leg(xg, args.batch_steps) if args.batch_steps > 0 else None
