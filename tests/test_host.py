@@ -37,6 +37,11 @@ def test_config_units_and_keys():
     assert c3.geometry == xg.XF_GEOM_MAA and c3.pbins == 64
     c2 = xg.Parser(os.path.join(CONFIGS, "config2_ma_mixed.txt"))
     assert c2.precision == xg.XF_PREC_MIXED
+    text = open(os.path.join(CONFIGS, "config0_ma.txt")).read()
+    for word, prec in (("df", xg.XF_PREC_DF), ("DF", xg.XF_PREC_DF), ("mixed", xg.XF_PREC_MIXED)):
+        assert xg.Config.from_text(text.replace("precision= fp64", "precision= " + word)).precision == prec
+    with pytest.raises(xg.XflatError):
+        xg.Config.from_text(text.replace("precision= fp64", "precision= fp16"))
     sa = xg.Parser(os.path.join(CONFIGS, "sa_bulb.txt"))
     assert sa.geometry == xg.XF_GEOM_SA and sa.ebins == 512
 
