@@ -21,10 +21,14 @@ def golden(name):
 
 
 def golden_names(kind):
+    """Window fixtures of make_golden.py with output `kind` (the whole-run
+    fixture of make_full_run.py carries no meta and is read by its own test)."""
     names = []
     for f in sorted(os.listdir(GOLDEN)):
         if f.endswith(".npz"):
             g = np.load(os.path.join(GOLDEN, f))
+            if "meta" not in g.files:
+                continue
             meta = json.loads(bytes(g["meta"]).decode())
             if kind in meta["outputs"].split():
                 names.append(f[:-4])

@@ -108,3 +108,20 @@ def test_free_running_loop_matches_reference(name):
     assert out["accepted"] == len(log)
     np.testing.assert_array_equal(out["log"][:, 0], log[:, 0])
     np.testing.assert_allclose(out["log"][:, 2], log[:, 2], rtol=1e-5)
+
+
+def test_whole_run_fixture():
+    """The reference's whole config-0 run (tests/golden/make_full_run.py), the
+    target of tests/test_gpu_full_run.py: made from the configuration file as
+    it is now, with the noise the GPU runs use, ending at Rn."""
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cfg = os.path.join(root, "xflat_gb300", "configs", "config0_ma.txt")
+    ref = np.load(os.path.join(root, "tests", "golden", "c0_full_ref.npz"))
+    text = str(ref["config"])
+    assert text == open(cfg).read()
+    assert int(ref["seed"]) == key(text, "seed", int) and float(ref["noise_amp"]) == key(text, "noise_amp")
+    assert float(ref["r_end"]) == key(text, "Rn")
+    assert ref["pee"].shape == (key(text, "Abins", int), key(text, "Ebins", int))
+    assert np.all((ref["pee"] >= 0.) & (ref["pee"] <= 1.))
+    assert int(ref["accepted"]) <= int(ref["iterations"]) < key(text, "Ts", int)
