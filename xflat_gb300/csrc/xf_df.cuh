@@ -14,7 +14,8 @@
 // sigma(h) (q = 1, or 1/2 for the halved forms): C - 1 = t c1(t) and
 // S = dl (1 + t s1(t)) with t = |h|^2 dl^2, whose leading constants are
 // pairs; when t <= 1e-3 in the whole warp (the bulb run's steps) the rest of
-// c1 and s1 is an FP32 tail below 3e-15 of C and S, otherwise the series is
+// c1 and s1 is an FP32 tail, which with the FP32 rounding of t in it changes
+// C and S by less than 5e-15 (3.1e-15 at t = 1e-3), otherwise the series is
 // a pair Horner up to t = 0.25 and FP64 sincos beyond.
 //
 // The per-beam Hamiltonian offsets are formed in FP64 (two operations per
@@ -144,9 +145,9 @@ __device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DBeam
     DK k;
     if (__all_sync(kFull, t.h <= 1e-3f)) {
         // tails t (1/24 - t/720) and t (1/120 - t/5040) in FP32: below 4.2e-5
-        // and 8.4e-6, rounded to 2^-24 of that; the next terms, t^3/40320 and
-        // t^3/362880, are below 2.5e-14 and 2.8e-15 of c1 and s1, and enter C
-        // and S times t
+        // and 8.4e-6, rounded to 2^-24 of that and computed from t rounded to
+        // FP32; the next terms, t^3/40320 and t^3/362880, are below 2.5e-14
+        // and 2.8e-15 of c1 and s1; all of it enters C and S times t
         const float th = t.h;
         c1 = fast_two_sum(-0.5f, th * fmaf(th, -1.f / 720.f, 1.f / 24.f));
         s1 = df_add(dconst(kDS[0]), DF{th * fmaf(th, -1.f / 5040.f, 1.f / 120.f), 0.f});
