@@ -142,7 +142,7 @@ int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins)
 /* Tuning and diagnostics, no reference counterpart: "threads" / "blocks" set
  * the launch shape of the phase kernels (0 = default); "renorm_every" sets
  * the accepted steps between the mixed path's unitarity renormalisations
- * (default 16, 0 = never); "prefetch" sets how many energy-loop iterations
+ * (default 16, 0 = never; the double-float path takes 0 only); "prefetch" sets how many energy-loop iterations
  * ahead the mixed path's phase kernels prefetch the state rows into L1
  * (default 1, 0 = none); "debug_psi3" = 1 makes
  * the last phase also store U(h4, dl2) psi3 into psi3, as the reference's

@@ -125,6 +125,9 @@ def test_unitarity_without_renormalisation():
 
 
 def test_unsupported_combinations():
+    s = xg.Simulation(xg.Config.from_text(_df(derive("config0_ma.txt", Abins=8, Ebins=16))))
+    assert s.lib.xf_set_option(s.h, b"renorm_every", 16.0) == xg._abi.XF_EUNSUPPORTED
+    assert s.lib.xf_set_option(s.h, b"renorm_every", 0.0) == 0
     with pytest.raises(xg.XflatError):
         xg.Simulation(xg.Config.from_text(_df(derive("config3_maa.txt", Abins=8, Pbins=4, Ebins=16))))
     with pytest.raises(xg.XflatError):

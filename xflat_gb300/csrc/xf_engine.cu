@@ -702,6 +702,8 @@ int xf_set_option(xf_handle* h, const char* name, double value)
         h->debug_psi3 = value != 0.;
     } else if (n == "renorm_every") {
         if (value < 0.) return h->fail(XF_EINVAL, "renorm_every must be >= 0");
+        if (h->dev.df && value > 0.)
+            return h->fail(XF_EUNSUPPORTED, "the double-float path keeps |a|^2 + |b|^2 = 1 without renormalisation");
         h->renorm_every = (int)value;
     } else if (n == "prefetch") {
         if (value < 0. || value > 8.) return h->fail(XF_EINVAL, "prefetch must be in [0, 8]");
