@@ -167,10 +167,18 @@ def cpu_baseline(text, r0, dr0, target_s=15.0):
                       % (res["iterations"], r0, res["seconds"])}
 
 
+def workload_config():
+    """The `config` of both arms' lines: the same workload, the same start."""
+    return {"workload": WORKLOAD, "bins": 2048 * 4 * 512, "r0_km": R_START, "dr0_km": DR_START,
+            "start": "seeded noise state (seed 1, amplitude 1e-7) at r0; every timed run starts there",
+            "l2": "inputs larger than L2 (four 134 MB state buffers)"}
+
+
 def reference_arm(args, rank):
     """CPU implementation of the path on this host's cores: the reference built
     from its own sources (oracle/_ref) where it exists and runs, else the
-    oracle's C restatement of it."""
+    oracle's C restatement of it.  Like the GPU arm, the warm-up and the timed
+    run each start from the workload's start state at r0."""
     if rank != 0:
         return 0
     text = workload_text(R0=R_START, dr=DR_START)
@@ -213,14 +221,195 @@ def reference_arm(args, rank):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": it, "warmup": args.warmup,
         "ms_per_step": 1e3 * secs / it, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD, "bins": bins, "parallelism": "OpenMP over angle bins, host cores"},
+        "dtype": "f64", "data": "synthetic", "impl": "reference", "config": workload_config(),
+        "parallelism": "OpenMP over angle bins, host cores",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": "%d stepper iterations of the workload, loop wall time" % it},
+                         "sample": "%d stepper iterations of the workload from r0, loop wall time" % it},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def pee(psi):
+    """P_ee(E) = |a(E)|^2 of the nu_e beams (particle index 0)."""
+    x = psi[0::4]
+    return x[:, 0] ** 2 + x[:, 1] ** 2
+
+
+def set_precision(text, prec):
+    return re.sub(r"^precision=.*$", "precision= " + prec, text, flags=re.M)
+
+
+def replay_inputs(r0, log):
+    """(r_before, dr) of a run's accepted steps, in order (r += dr, src/Nmr.cpp:229)."""
+    import numpy as np
+    rb = np.concatenate([[r0], log[:-1, 1]]) if len(log) else np.zeros(0)
+    return rb, log[:, 2].copy()
+
+
+def accuracy_vs(xg, text, prec, psi_start, r0, log, psi_ref, surv_ref):
+    """The run forced onto the FP64 run's accepted steps in precision `prec`
+    (xf_replay): max |dP_ee(E)| over every nu_e beam and max per-beam
+    survival-probability error (the src/IO_f.cpp:341-351 quantity) against
+    FP64 at the same radius.  Always computed, whatever steps the free-running
+    variant took."""
+    import numpy as np
+    m = xg.Simulation(xg.Config.from_text(set_precision(text, prec)))
+    m.set_state(psi_start)
+    rb, dr = replay_inputs(r0, log)
+    m.replay(rb, dr)
+    out = {"max_dPee_vs_fp64": float(np.max(np.abs(pee(m.get_state(0)) - pee(psi_ref)))),
+           "max_dsurvival_vs_fp64": float(np.max(np.abs(m.survival() - surv_ref))),
+           "compared_on": "the FP64 run's %d accepted steps replayed" % len(rb)}
+    m.close()
+    return out
+
+
+def timed_run(xg, text, psi_start, r0, dr0, steps, warmup, log=False, options=None):
+    """Device-controlled run of `steps` iterations from (r0, dr0) and the
+    start state, after `warmup` iterations from the same start."""
+    sim = xg.Simulation(xg.Config.from_text(text))
+    for k, v in (options or {}).items():
+        sim.lib.xf_set_option(sim.h, k.encode(), float(v))
+    sim.set_state(psi_start)
+    sim.evolutionLoop(max_iters=max(3, warmup), device_control=True, iters_per_launch=16, r0=r0, dr0=dr0)
+    sim.set_state(psi_start)
+    out = sim.evolutionLoop(max_iters=steps, device_control=True, iters_per_launch=16, r0=r0, dr0=dr0,
+                            time_phases=True, log_cap=steps if log else 0)
+    return sim, out
+
+
+VARIANT_WORKLOAD = {
+    "mixed": "precision= mixed (FP32 rotations and compensated FP32 state; FP64 moment reduction, error estimate, "
+             "control, renormalisation)",
+    "df": "precision= df (every state, propagator, average and moment in double-float FP32 pairs; FP64 block "
+          "reduction and control)",
+}
+
+
+def variant_leg(xg, prec, text, psi_start, r0, dr0, steps, bins, log64, psi64, surv64, st64, warmup=3):
+    """The same K steps from the same state in another precision: speed of the
+    free run, accuracy on FP64's own accepted steps."""
+    m, out = timed_run(xg, set_precision(text, prec), psi_start, r0, dr0, steps, warmup)
+    ms, _ = m.phase_times()
+    m.close()
+    res = {"value": bins * out["iterations"] / (out["device_ms"] * 1e-3), "unit": UNIT,
+           "ms_per_step": out["device_ms"] / max(1, out["iterations"]), "phases_ms": dict(zip("ABC", map(float, ms))),
+           "iterations": out["iterations"], "accepted": out["accepted"], "accepted_fp64": st64["accepted"],
+           "speedup_vs_fp64": None, "workload": VARIANT_WORKLOAD[prec]}
+    res.update(accuracy_vs(xg, text, prec, psi_start, r0, log64, psi64, surv64))
+    return res
+
+
+def shape_leg(xg, name, text, r0, dr0, steps, warmup):
+    """FP64, mixed and double-float on one workload shape: ms per iteration and
+    bin-iterations per second of each, accuracy of the others against FP64 on
+    FP64's accepted steps."""
+    sim = xg.Simulation(xg.Config.from_text(text))
+    psi0 = sim.get_state(0).copy()
+    bins = sim.nbeams * sim.ebins
+    sim.close()
+    s64, o64 = timed_run(xg, text, psi0, r0, dr0, steps, warmup, log=True)
+    psi64, surv64 = s64.get_state(0).copy(), s64.survival().copy()
+    s64.close()
+    out = {"workload": name, "bins": bins, "r0_km": r0, "r_end_km": o64["r_end"], "iterations": o64["iterations"],
+           "fp64": {"ms_per_step": o64["device_ms"] / max(1, o64["iterations"]),
+                    "value": bins * o64["iterations"] / (o64["device_ms"] * 1e-3)}}
+    for prec in ("mixed", "df"):
+        v = variant_leg(xg, prec, text, psi0, r0, dr0, steps, bins, o64["log"], psi64, surv64, o64, warmup)
+        v["speedup_vs_fp64"] = v["value"] / out["fp64"]["value"]
+        out[prec] = v
+    return out
+
+
+def long_window_leg(xg, iters):
+    """Double-float (and mixed) against FP64 over a long free-running window of
+    the config-0 physics (256 x 4 x 64 bins from r = 50 km): the step
+    sequences and max |dP_ee(E)| at the end, replayed on FP64's steps where
+    the free runs' step counts differ."""
+    import numpy as np
+    text = workload_text(os.path.join(ROOT, "xflat_gb300", "configs", "config0_ma.txt"), R0=50, dr="1.5e-4")
+    a = xg.Simulation(xg.Config.from_text(text))
+    psi0 = a.get_state(0).copy()
+    oa = a.evolutionLoop(max_iters=iters, device_control=True, log_cap=iters)
+    pa, sa = a.get_state(0).copy(), a.survival().copy()
+    a.close()
+    out = {"workload": "config-0 physics, 256 x 4 x 64 bins, free-running from r = 50 km",
+           "iterations": oa["iterations"], "r_km": [50.0, oa["r_end"]], "fp64_seconds": oa["device_ms"] * 1e-3}
+    for prec in ("df", "mixed"):
+        b = xg.Simulation(xg.Config.from_text(set_precision(text, prec)))
+        ob = b.evolutionLoop(max_iters=iters, device_control=True)
+        same = (ob["iterations"], ob["accepted"]) == (oa["iterations"], oa["accepted"]) and ob["r_end"] == oa["r_end"]
+        res = {"accepted": ob["accepted"], "accepted_fp64": oa["accepted"], "same_step_sequence_end": same,
+               "seconds": ob["device_ms"] * 1e-3}
+        if same:
+            res["max_dPee_vs_fp64"] = float(np.max(np.abs(pee(b.get_state(0)) - pee(pa))))
+            res["max_dsurvival_vs_fp64"] = float(np.max(np.abs(b.survival() - sa)))
+            res["compared_on"] = "free runs ending at the same radius after the same steps"
+        else:
+            res.update(accuracy_vs(xg, text, prec, psi0, 50.0, oa["log"][:oa["accepted"]], pa, sa))
+        b.close()
+        out[prec] = res
+    return out
+
+
+def batched_leg(xg, steps):
+    """The batched parameter sweep (64 independent MA instances from a seed,
+    xflat_gb300.sweep): double-float, mixed precision and FP64 in one batch
+    each, and the same 64 instances run back to back through the
+    single-simulation FP64 path."""
+    import numpy as np
+    from xflat_gb300.sweep import sweep_configs
+    out = {"workload": "64 MA instances (seed 4): angle bins U{128..2048}, energy bins U{32..512} (1-60 MeV), "
+                       "L log-U[1e50,1e52] erg/s, NH/IH p=1/2, lambda0 log-U[1e2,1e4] /km, from r=10 km",
+           "steps_per_instance": steps}
+    states = {}
+    for prec in ("df", "mixed", "fp64"):
+        b = xg.Batch([xg.Config.from_text(t) for t in sweep_configs(seed=4, n=64, precision=prec)])
+        r = b.run(max_iters=steps)
+        units = sum(nb * ne * i for (nb, ne), i in zip(b.dims, r["iterations"]))
+        out["bins"] = sum(nb * ne for nb, ne in b.dims)
+        t = b.tuning()
+        out["batched_" + prec] = {"value": units / r["seconds"], "unit": UNIT, "seconds": r["seconds"],
+                                  "tile": {"warps_per_block": t["warps"], "beams_per_warp": t["beams_per_warp"],
+                                           "candidates_ms": {"%dx%d" % (w, bp): round(ms, 3)
+                                                             for w, bp, ms in t["candidates"]}}}
+        states[prec] = ([b.get_state(i)[0::4, :2] for i in range(len(b.dims))], list(r["accepted"]))
+        b.close()
+    units, ms = 0, 0.0
+    for t in sweep_configs(seed=4, n=64, precision="fp64"):
+        s = xg.Simulation(xg.Config.from_text(t))
+        o = s.evolutionLoop(max_iters=steps, device_control=True)
+        units += s.nbeams * s.ebins * o["iterations"]
+        ms += o["device_ms"]
+        s.close()
+    out["fp64_back_to_back"] = {"value": units / (ms * 1e-3), "unit": UNIT}
+    for prec in ("df", "mixed"):
+        out["speedup_batched_%s_vs_fp64_back_to_back" % prec] = (out["batched_" + prec]["value"] /
+                                                                 out["fp64_back_to_back"]["value"])
+        d, diverged = [], 0
+        for a, c, na, nc in zip(states["fp64"][0], states[prec][0], states["fp64"][1], states[prec][1]):
+            if na != nc:
+                diverged += 1
+                continue
+            d.append(np.max(np.abs((a[:, 0] ** 2 + a[:, 1] ** 2) - (c[:, 0] ** 2 + c[:, 1] ** 2))))
+        out["max_dPee_batched_%s_vs_fp64" % prec] = float(max(d)) if d else None
+        out["instances_compared_" + prec] = len(d)
+        out["instances_with_other_step_count_" + prec] = diverged
+    return out
+
+
+def whole_run_record():
+    """The opt-in whole-run test's measured result (tests/test_gpu_full_run.py),
+    committed as profiles/whole_run_config0.json: recorded, not measured by
+    this run."""
+    path = os.path.join(ROOT, "profiles", "whole_run_config0.json")
+    if not os.path.exists(path):
+        return None
+    rec = json.load(open(path))
+    rec["source"] = "profiles/whole_run_config0.json (tests/test_gpu_full_run.py on a GB300; not measured by this run)"
+    return rec
 
 
 def ours(args, rank, world, dist):
@@ -232,17 +421,18 @@ def ours(args, rank, world, dist):
     sim = xg.Simulation(xg.Config.from_text(text))
     bins = sim.nbeams * sim.ebins
     state_bytes = bins * 4 * 8
-
-    # --- warm-up, then the timed region: K device-controlled iterations with the
-    # inputs resident in HBM (4 state buffers of 134 MB each: larger than L2)
-    w = sim.evolutionLoop(max_iters=max(3, args.warmup), device_control=True, iters_per_launch=16)
-    r0, dr0 = w["r_end"], w["dr_end"]
     psi_start = sim.get_state(0).copy()
+
+    # --- warm-up, then the timed region: K device-controlled iterations from the
+    # start state at r0 with the inputs resident in HBM (4 state buffers of 134
+    # MB each: larger than L2)
+    sim.evolutionLoop(max_iters=max(3, args.warmup), device_control=True, iters_per_launch=16)
+    sim.set_state(psi_start)
     if dist:
         dist.barrier()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
         st = sim.evolutionLoop(max_iters=args.steps, device_control=True, iters_per_launch=min(16, args.steps),
-                               r0=r0, dr0=dr0, time_phases=True)
+                               r0=R_START, dr0=DR_START, time_phases=True, log_cap=args.steps)
     if dist:
         dist.barrier()
     phase_ms, phase_n = sim.phase_times()
@@ -250,13 +440,7 @@ def ours(args, rank, world, dist):
     units = bins * st["iterations"]
     psi_fp64_end = sim.get_state(0).copy()
     surv_fp64 = sim.survival()
-
-    # --- mixed precision (FP32 rotations and compensated FP32 state, FP64
-    # reductions/control) and double-float (every operation in FP32 pairs) on
-    # the same workload: same start state, same K steps
-    mixed = variant_leg(xg, "mixed", text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
-    dfl = variant_leg(xg, "df", text, psi_start, r0, dr0, args.steps, bins, psi_fp64_end, surv_fp64, st)
-    batched = batched_leg(xg, args.batch_steps) if args.batch_steps > 0 else None
+    log64 = st["log"][:st["accepted"]]
 
     # --- end to end through the C ABI with host buffers: state H2D from pinned
     # memory (xf_set_state), the loop through xf_run, state D2H into pinned
@@ -268,13 +452,13 @@ def ours(args, rank, world, dist):
     # iteration r, dr and the three matter terms H2D, Max_err D2H) is reported
     # beside it.
     host_psi, pinned = pinned_empty(bins * 4)
-    sim.get_state(0, out=host_psi)
+    host_psi[:] = psi_start.reshape(-1)
     out = pinned_empty(bins * 4)[0]
 
     def end_to_end(device_control):
         t0 = time.perf_counter()
         sim.set_state(host_psi)
-        e = sim.evolutionLoop(max_iters=args.steps, device_control=device_control, r0=r0, dr0=dr0)
+        e = sim.evolutionLoop(max_iters=args.steps, device_control=device_control, r0=R_START, dr0=DR_START)
         sim.get_state(0, out=out)
         return time.perf_counter() - t0, e
 
@@ -282,6 +466,7 @@ def ours(args, rank, world, dist):
     e2e_units = bins * e["iterations"]
     hd_s, ehd = end_to_end(False)
     hd_value = bins * ehd["iterations"] / hd_s
+    sim.close()
 
     # --- aggregation over replicas
     if dist:
@@ -298,6 +483,32 @@ def ours(args, rank, world, dist):
     if rank != 0:
         return 0
 
+    # --- the same K steps in the other precisions (speed of the free runs,
+    # accuracy on FP64's accepted steps), normal hierarchy, the other
+    # workload shapes, a long window, the batched sweep
+    variants = {"fp64": {"value": value, "unit": UNIT}}
+    for prec in ("mixed", "df"):
+        v = variant_leg(xg, prec, text, psi_start, R_START, DR_START, args.steps, bins, log64, psi_fp64_end,
+                        surv_fp64, st)
+        v["speedup_vs_fp64"] = v["value"] / value
+        variants[prec] = v
+    extra = {}
+    if not args.quick:
+        nh = workload_text(R0=R_START, dr=DR_START, dm2="3E-3")
+        extra["normal_hierarchy"] = shape_leg(
+            xg, "as the FP64 line with normal hierarchy (dm2 = +3e-3 eV^2)", nh, R_START, DR_START,
+            min(args.steps, 50), 3)
+        extra["config0_shape"] = shape_leg(
+            xg, "config-0 physics, 256 x 4 x 64 bins (65,536; 1e51 erg/s), from r = 10 km: latency-bound",
+            workload_text(os.path.join(ROOT, "xflat_gb300", "configs", "config0_ma.txt")), 10.0, 1e-3,
+            2000, 10)
+        extra["maa_config3"] = shape_leg(
+            xg, "MAA 256 polar x 64 azimuthal x 4 x 128 energy bins (8.39 M; 1e51 erg/s, IH), from r = 50 km",
+            workload_text(os.path.join(ROOT, "xflat_gb300", "configs", "config3_maa.txt"), R0=50, dr="1e-4"),
+            50.0, 1e-4, min(args.steps, 40), 3)
+        extra["long_window"] = long_window_leg(xg, args.window)
+    batched = batched_leg(xg, args.batch_steps) if args.batch_steps > 0 else None
+
     # --- roofline of the dominant phase kernel against the live FP64 FMA peak
     peak = lib_peak(lib)
     totals = {p: phase_ms[i] * phase_n[i] for i, p in enumerate("ABC")}
@@ -313,24 +524,24 @@ def ours(args, rank, world, dist):
         peaks = json.load(open(pk_path))
     hbm_peak = peaks.get("hbm_gbs")
 
-    cpu = cpu_baseline(text, r0, dr0) if not args.skip_cpu else None
+    cpu = cpu_baseline(text, R_START, DR_START) if not args.skip_cpu else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": st["iterations"],
         "warmup": max(3, args.warmup), "ms_per_step": 1e3 * tmax / max(1, st["iterations"]),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bins": bins, "precision": "fp64", "stepping": "device-controlled",
-                   "accepted": st["accepted"], "r_range_km": [r0, st["r_end"]],
-                   "l2": "inputs larger than L2 (four 134 MB state buffers per replica)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(),
+        "run": {"precision": "fp64", "stepping": "device-controlled", "accepted": st["accepted"],
+                "r_range_km": [R_START, st["r_end"]], "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": PHASE_KERNEL[dom],
                      "peak_source": "FP64 FMA throughput measured live by xf_probe_fp64_peak",
+                     "traffic_source": "ncu capture summarised in profiles/%s_config1.md" % PHASE_KERNEL[dom],
                      "ops_per_bin": PHASE_OPS[dom],
                      "hbm_view": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak,
                                   "frac": hbm_achieved / hbm_peak if hbm_peak else None,
                                   "algorithmic_bytes_per_bin": PHASE_BYTES[dom]}},
         "phases_ms": {p: phase_ms[i] for i, p in enumerate("ABC")},
-        "variants": {"fp64": {"value": value, "unit": UNIT}, "mixed": mixed, "df": dfl, "batched": batched},
+        "variants": variants, "workloads": extra, "batched": batched, "whole_run": whole_run_record(),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": (state_bytes + e["h2d_bytes"]) /
                 max(1, e["iterations"]), "d2h_bytes_per_step": (state_bytes + e["d2h_bytes"]) /
@@ -345,75 +556,6 @@ def ours(args, rank, world, dist):
     }
     print(json.dumps(line), flush=True)
     return 0
-
-
-def pee(psi):
-    """P_ee(E) = |a(E)|^2 of the nu_e beams (particle index 0)."""
-    x = psi[0::4]
-    return x[:, 0] ** 2 + x[:, 1] ** 2
-
-
-VARIANT_WORKLOAD = {
-    "mixed": "same as the FP64 line, precision= mixed (FP32 rotations and compensated FP32 state; "
-             "FP64 moment reduction, error estimate, control, renormalisation)",
-    "df": "same as the FP64 line, precision= df (every state, propagator, average and moment in double-float "
-          "FP32 pairs; FP64 block reduction and control)",
-}
-
-
-def variant_leg(xg, prec, text, psi_start, r0, dr0, steps, bins, psi_fp64_end, surv_fp64, st64):
-    """Run of the same K steps from the same state in another precision;
-    accuracy against the FP64 run: max |dP_ee(E)| over every nu_e beam and max
-    per-beam survival-probability error (src/IO_f.cpp:341-351 quantity)."""
-    import numpy as np
-    m = xg.Simulation(xg.Config.from_text(text.replace("precision= fp64", "precision= " + prec)))
-    m.set_state(psi_start)
-    out = m.evolutionLoop(max_iters=steps, device_control=True, iters_per_launch=min(16, steps), r0=r0, dr0=dr0)
-    res = {"value": bins * out["iterations"] / (out["device_ms"] * 1e-3), "unit": UNIT,
-           "ms_per_step": out["device_ms"] / max(1, out["iterations"]), "iterations": out["iterations"],
-           "accepted": out["accepted"], "accepted_fp64": st64["accepted"], "workload": VARIANT_WORKLOAD[prec]}
-    if out["accepted"] == st64["accepted"]:
-        res["max_dPee_vs_fp64"] = float(np.max(np.abs(pee(m.get_state(0)) - pee(psi_fp64_end))))
-        res["max_dsurvival_vs_fp64"] = float(np.max(np.abs(m.survival() - surv_fp64)))
-    m.close()
-    return res
-
-
-def batched_leg(xg, steps):
-    """The batched parameter sweep (64 independent MA instances from a seed,
-    xflat_gb300.sweep): mixed precision and FP64 in one batch each, and the same
-    64 instances run back to back through the single-simulation FP64 path."""
-    import numpy as np
-    from xflat_gb300.sweep import sweep_configs
-    out = {"workload": "64 MA instances (seed 4): angle bins U{128..2048}, energy bins U{32..512} (1-60 MeV), "
-                       "L log-U[1e50,1e52] erg/s, NH/IH p=1/2, lambda0 log-U[1e2,1e4] /km, from r=10 km",
-           "steps_per_instance": steps}
-    states = {}
-    for prec in ("mixed", "fp64"):
-        b = xg.Batch([xg.Config.from_text(t) for t in sweep_configs(seed=4, n=64, precision=prec)])
-        r = b.run(max_iters=steps)
-        units = sum(nb * ne * i for (nb, ne), i in zip(b.dims, r["iterations"]))
-        out["bins"] = sum(nb * ne for nb, ne in b.dims)
-        out["batched_" + prec] = {"value": units / r["seconds"], "unit": UNIT, "tile_warps": b.tile_shape()[0],
-                                  "seconds": r["seconds"]}
-        states[prec] = ([b.get_state(i)[0::4, :2] for i in range(len(b.dims))], list(r["accepted"]))
-        b.close()
-    units, ms = 0, 0.0
-    for t in sweep_configs(seed=4, n=64, precision="fp64"):
-        s = xg.Simulation(xg.Config.from_text(t))
-        o = s.evolutionLoop(max_iters=steps, device_control=True)
-        units += s.nbeams * s.ebins * o["iterations"]
-        ms += o["device_ms"]
-        s.close()
-    out["fp64_back_to_back"] = {"value": units / (ms * 1e-3), "unit": UNIT}
-    out["speedup_batched_mixed_vs_fp64_back_to_back"] = out["batched_mixed"]["value"] / out["fp64_back_to_back"]["value"]
-    d = []
-    for a, c, na, nc in zip(states["fp64"][0], states["mixed"][0], states["fp64"][1], states["mixed"][1]):
-        if na == nc:
-            d.append(np.max(np.abs((a[:, 0] ** 2 + a[:, 1] ** 2) - (c[:, 0] ** 2 + c[:, 1] ** 2))))
-    out["max_dPee_batched_mixed_vs_fp64"] = float(max(d)) if d else None
-    out["instances_compared"] = len(d)
-    return out
 
 
 def lib_peak(lib):
@@ -431,6 +573,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline leg")
     ap.add_argument("--batch-steps", type=int, default=24, help="iterations per instance of the batched legs (0 = skip)")
+    ap.add_argument("--window", type=int, default=100000,
+                    help="iterations of the long double-float/mixed vs FP64 window at the config-0 shape")
+    ap.add_argument("--quick", action="store_true", help="omit the other workload shapes and the long window")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

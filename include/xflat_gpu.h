@@ -12,10 +12,11 @@
  *   include/Fio.h:22-38    fio::init, fillInitData, dumpToFile, freemem
  *   include/Matt.h:22-36   matt::init, getHm
  *   include/Parser.h:9-28  Parser(configFile)
- * This header replaces that contract with handle-based entry points.  All
+ * This header replaces that contract with handle-based entry points.  The
  * buffers crossing the ABI are host memory in the reference's NetCDF psi
  * layout [theta][phi][prtcl][comp][ebin] (src/IO_f.cpp:280-288), copied
- * synchronously; no device pointers and no C++ types cross it.  Every entry
+ * synchronously, with one exception: xf_calc_hvv_static takes caller-owned
+ * device pointers and a CUDA stream.  No C++ types cross the ABI.  Every entry
  * point returns an xf_status; none exits or traps.  Calls on one handle must
  * come from one thread at a time; handles are independent.
  */
@@ -55,7 +56,7 @@ enum { XF_PREC_FP64 = 0, XF_PREC_MIXED = 1, XF_PREC_DF = 2 };
  * reference leaves them uninitialized). */
 typedef struct xf_config {
     int geometry;        /* XF_GEOM_*  (extension key "geometry= MA|MAA|SA") */
-    int precision;       /* XF_PREC_*  (extension key "precision= fp64|mixed|df"; df: MA and SA) */
+    int precision;       /* XF_PREC_*  (extension key "precision= fp64|mixed|df") */
     int abins, pbins, ebins, flvs;
     int has_matter;      /* hasMatter= */
     int dump_mode;       /* dumpMode= (bit 1 snapshot file, bit 2 probability file) */
@@ -140,13 +141,16 @@ const char* xf_last_error(const xf_handle* h);
 /* nbeams = theta*phi*4 (phy::beamLen, src/Phy_MA.cpp:78). */
 int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins);
 /* Tuning and diagnostics, no reference counterpart: "threads" / "blocks" set
- * the launch shape of the phase kernels (0 = default); "renorm_every" sets
- * the accepted steps between the mixed path's unitarity renormalisations
- * (default 16, 0 = never; the double-float path takes 0 only); "prefetch" sets how many energy-loop iterations
- * ahead the mixed path's phase kernels prefetch the state rows into L1
- * (default 1, 0 = none); "debug_psi3" = 1 makes
- * the last phase also store U(h4, dl2) psi3 into psi3, as the reference's
- * in-place stage S10 does (src/Nmr.cpp:191). */
+ * the launch shape of the phase kernels (0 = default; the double-float
+ * default is one wave of resident blocks per phase); "renorm_every" sets the
+ * accepted steps between the mixed path's unitarity renormalisations
+ * (default 16, 0 = never; the double-float path takes 0 only); "prefetch"
+ * sets how many energy-loop iterations ahead the mixed and double-float phase
+ * kernels prefetch the state rows into L1 (default 1, 0 = none);
+ * "df_b_occupancy" (2 or 3, default 3) picks the double-float phase-B kernel
+ * built for that many resident blocks per SM; "debug_psi3" = 1 makes the last
+ * phase also store U(h4, dl2) psi3 into psi3, as the reference's in-place
+ * stage S10 does (src/Nmr.cpp:191). */
 int xf_set_option(xf_handle* h, const char* name, double value);
 
 /* ---------------------------------------------------------------- state */
@@ -207,7 +211,9 @@ int xf_survival(xf_handle* h, double* out);
  * abins*pbins*4 <= 65536 beams (larger sizes return XF_EINVAL).  The first call
  * on a device looks that array up (make it before any stream capture); calls
  * that overlap on the GPU race on the shared array.  Work is queued on
- * `stream` (a cudaStream_t, NULL for the default stream). */
+ * `stream` (a cudaStream_t of the current device, NULL for the default
+ * stream; a stream of another device returns XF_EINVAL).  A CUDA error
+ * already pending on entry returns XF_ECUDA and stays pending. */
 int xf_calc_hvv_static(int geometry, int abins, int pbins, int ebins, int epad, const double* psi,
                        const double* fv, const double* cosb, const double* sinb, const double* dcosb,
                        const double* cosphi, const double* sinphi, const double* LE, double kappa,
@@ -253,7 +259,7 @@ int xf_snapshot_read(const char* path, long rec, double* r, double* dr, double* 
 /* Many independent simulations with per-instance adaptive steps, advanced
  * together by the same phase kernels (one launch per phase covers every
  * instance), captured in CUDA graphs.  Configs may be MA or SA (they share
- * the MA-shaped kernels) and must share precision. */
+ * the MA-shaped kernels) and must share precision (fp64, mixed or df). */
 typedef struct xf_batch xf_batch;
 int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out);
 int xf_batch_destroy(xf_batch* b);
@@ -264,9 +270,19 @@ int xf_batch_get_state(xf_batch* b, int inst, double* psi);
 /* Advance every unfinished instance by up to max_iters iterations (< 0: each
  * instance's Ts); per-instance results in iters/accepted/r_end (may be NULL). */
 int xf_batch_run(xf_batch* b, long max_iters, long* iters, long* accepted, double* r_end, double* seconds);
-/* Beams per tile chosen by the autotuner at creation, and the measured time
- * (ms, 8 iterations) of each candidate tile shape {2, 4, 8} (may be NULL). */
+/* Warps per block chosen by the autotuner at creation, and the measured time
+ * (ms, 8 iterations) of the candidates {2, 4, 8} warps with one beam per warp
+ * (may be NULL). */
 int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms);
+/* The autotuner's full table: the chosen warps per block (block size 32 x
+ * warps) and beams per warp (blocks per phase = beams / (warps x beams per
+ * warp)), and for each of the *ncand (<= 16) candidates its shape and the
+ * measured time (ms, 8 iterations of the whole batch).  Any output may be NULL. */
+int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* ncand, int* cand_warps, int* cand_bpw,
+                    double* cand_ms);
+/* Replaces the tuned tile shape: warps per block in [1, 8], beams per warp in
+ * [1, 64]. */
+int xf_batch_set_shape(xf_batch* b, int warps, int beams_per_warp);
 
 #ifdef __cplusplus
 }

@@ -121,7 +121,8 @@ def run_case(name, base, overrides, amp, outputs, refdir, tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("XFLAT_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference"),
+                    help="reference checkout (default: XFLAT_REFERENCE, else `reference` beside the repository)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + args.ref, "-j8"], check=True,

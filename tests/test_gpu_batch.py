@@ -39,6 +39,26 @@ def test_batch_uneven_budgets_and_radii():
     assert all(out["iterations"][i] == 60 for i in (0, 2, 3))
     w, ms = b.tile_shape()
     assert w in (2, 4, 8) and np.all(ms > 0)
+    t = b.tuning()
+    assert len(t["candidates"]) == 9 and all(c[2] > 0 for c in t["candidates"])
+    assert (t["warps"], t["beams_per_warp"]) == min(t["candidates"], key=lambda c: c[2])[:2]
+
+
+@pytest.mark.parametrize("warps,bpw", [(2, 4), (8, 2)])
+def test_batch_tile_shapes_agree(warps, bpw):
+    """Every tile shape gives the same decisions and states (the per-instance
+    reductions are summed in an order fixed by the shape, so states agree to
+    rounding)."""
+    texts = _small_sweep()
+    b = xg.Batch([xg.Config.from_text(t) for t in texts])
+    ref = b.run(max_iters=40)
+    ref_states = [b.get_state(i) for i in range(len(texts))]
+    c = xg.Batch([xg.Config.from_text(t) for t in texts])
+    assert c.lib.xf_batch_set_shape(c.h, warps, bpw) == 0
+    out = c.run(max_iters=40)
+    assert list(out["accepted"]) == list(ref["accepted"])
+    for i in range(len(texts)):
+        assert pol_rel_err(c.get_state(i), ref_states[i]) <= 1e-10
 
 
 def test_batch_mixed_vs_fp64():
@@ -46,9 +66,11 @@ def test_batch_mixed_vs_fp64():
     b32 = xg.Batch([xg.Config.from_text(t) for t in _small_sweep("mixed")])
     o64 = b64.run(max_iters=80)
     o32 = b32.run(max_iters=80)
+    # every instance is compared: the step sequences must agree for the
+    # comparison to be at equal radii
+    assert list(o64["accepted"]) == list(o32["accepted"])
+    np.testing.assert_allclose(o32["r_end"], o64["r_end"], rtol=1e-9)
     for i in range(4):
-        if o64["accepted"][i] != o32["accepted"][i]:
-            continue
         a, c = b64.get_state(i), b32.get_state(i)
         pee = lambda x: x[0::4, 0] ** 2 + x[0::4, 1] ** 2
         assert np.max(np.abs(pee(a) - pee(c))) <= 1e-5
@@ -73,3 +95,29 @@ def test_batch_with_sa_instances():
         o = s.evolutionLoop(max_iters=60, device_control=True)
         assert (o["iterations"], o["accepted"]) == (out["iterations"][i], out["accepted"][i])
         assert pol_rel_err(b.get_state(i), s.get_state(0)) <= 1e-10
+
+
+def test_batch_df_equals_instances_run_alone():
+    """Double-float instances in a batch: the single-simulation double-float
+    path's decisions and states (moments summed in the batch's order)."""
+    texts = [t.replace("precision= fp64", "precision= df") for t in _small_sweep()]
+    b = xg.Batch([xg.Config.from_text(t) for t in texts])
+    out = b.run(max_iters=60)
+    for i, t in enumerate(texts):
+        s = xg.Simulation(xg.Config.from_text(t))
+        o = s.evolutionLoop(max_iters=60, device_control=True)
+        assert (o["iterations"], o["accepted"]) == (out["iterations"][i], out["accepted"][i])
+        assert pol_rel_err(b.get_state(i), s.get_state(0)) <= 1e-10
+
+
+def test_batch_df_vs_fp64():
+    b64 = xg.Batch([xg.Config.from_text(t) for t in _small_sweep("fp64")])
+    b2 = xg.Batch([xg.Config.from_text(t) for t in _small_sweep("df")])
+    o64 = b64.run(max_iters=80)
+    o2 = b2.run(max_iters=80)
+    assert list(o64["accepted"]) == list(o2["accepted"])
+    np.testing.assert_allclose(o2["r_end"], o64["r_end"], rtol=1e-9)
+    for i in range(4):
+        a, c = b64.get_state(i), b2.get_state(i)
+        pee = lambda x: x[0::4, 0] ** 2 + x[0::4, 1] ** 2
+        assert np.max(np.abs(pee(a) - pee(c))) <= 1e-8

@@ -1,5 +1,5 @@
 """Double-float path (precision= df: every state, propagator, average and
-moment as a pair of FP32 numbers, about 48 significant bits; MA and SA)
+moment as a pair of FP32 numbers, about 48 significant bits; MA, MAA and SA)
 against the reference's own outputs and the FP64 path.
 
 Bars: the reference's accepted-step sequence replayed, every beam's
@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import xflat_gb300 as xg
-from helpers import derive, golden, noise_state, pol_rel_err, replay_inputs
+from helpers import derive, golden, golden_names, noise_state, pol_rel_err, replay_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -39,7 +39,7 @@ def pee(psi):
     return x[:, 0] ** 2 + x[:, 1] ** 2
 
 
-@pytest.mark.parametrize("name", ["ma_small_r10", "ma_ragged_nh", "ma_small_r290", "ma_c0shape", "sa_r10", "sa_ragged"])
+@pytest.mark.parametrize("name", golden_names("replay"))
 def test_replay_reference_step_sequence(name):
     g = golden(name)
     sim = xg.Simulation(xg.Config.from_text(_df(g["config"])))
@@ -128,7 +128,49 @@ def test_unsupported_combinations():
     s = xg.Simulation(xg.Config.from_text(_df(derive("config0_ma.txt", Abins=8, Ebins=16))))
     assert s.lib.xf_set_option(s.h, b"renorm_every", 16.0) == xg._abi.XF_EUNSUPPORTED
     assert s.lib.xf_set_option(s.h, b"renorm_every", 0.0) == 0
-    with pytest.raises(xg.XflatError):
-        xg.Simulation(xg.Config.from_text(_df(derive("config3_maa.txt", Abins=8, Pbins=4, Ebins=16))))
-    with pytest.raises(xg.XflatError):
-        xg.Batch([xg.Config.from_text(_df(derive("config0_ma.txt", Abins=8, Ebins=16)))])
+
+
+# ------------------------------------------------------------------ MAA (16-scalar reduction)
+
+MAA = dict(Abins=16, Pbins=8, Ebins=32)
+
+
+@pytest.mark.parametrize("r,dr", [(12.0, 1.4e-6), (60.0, 2e-4), (40.0, 0.05)])
+def test_maa_one_iteration_vs_fp64(r, dr):
+    a, b = _pair(derive("config3_maa.txt", **MAA), 3, 1e-6)
+    me64, me2 = a.step(r, dr), b.step(r, dr)
+    assert abs(me2 - me64) <= 1e-5 * me64, (me2, me64)
+    a.accept()
+    b.accept()
+    assert np.max(np.abs(b.get_state(0) - a.get_state(0))) <= 1e-13
+
+
+@pytest.mark.parametrize("r0,iters", [(15.0, 300), (60.0, 200)])
+def test_maa_fp64_step_sequence_replayed(r0, iters):
+    text = derive("config3_maa.txt", R0=r0, dr="1e-6", **MAA)
+    a, b = _pair(text, 3, 1e-6)
+    oa = a.evolutionLoop(max_iters=iters, log_cap=iters)
+    rb, dr = replay_inputs(text, oa["log"][:oa["accepted"]])
+    b.replay(rb, dr)
+    assert pol_rel_err(b.get_state(0), a.get_state(0)) <= POL_TOL
+
+
+def test_maa_free_running_takes_fp64_decisions():
+    text = derive("config3_maa.txt", R0=15, dr="1e-6", **MAA)
+    a, b = _pair(text, 3, 1e-6)
+    oa = a.evolutionLoop(max_iters=300, log_cap=300, device_control=True)
+    ob = b.evolutionLoop(max_iters=300, log_cap=300, device_control=True)
+    assert (oa["iterations"], oa["accepted"]) == (ob["iterations"], ob["accepted"])
+    np.testing.assert_allclose(ob["log"][:, 2], oa["log"][:, 2], rtol=1e-4)
+    assert np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0)))) <= 1e-8
+
+
+def test_maa_workload_shape_window_vs_fp64():
+    """256 polar x 64 azimuthal x 4 x 128 energy bins (8.39 M): 6 iterations from 50 km."""
+    text = derive("config3_maa.txt", R0=50, dr="1e-4")
+    a, b = _pair(text, 3, 1e-6)
+    oa = a.evolutionLoop(max_iters=6, device_control=True)
+    ob = b.evolutionLoop(max_iters=6, device_control=True)
+    assert (oa["iterations"], oa["accepted"]) == (ob["iterations"], ob["accepted"])
+    assert abs(ob["last_max_err"] - oa["last_max_err"]) <= 1e-5 * oa["last_max_err"]
+    assert np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0)))) <= 1e-11

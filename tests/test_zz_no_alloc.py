@@ -7,14 +7,16 @@ output buffer, and the entry point's scratch is a fixed device array inside
 the library.  Its result is checked through the C ABI against the existing
 entry point xf_calc_hvv, on two calls in a row and after the state changed.
 This file is collected last so that a run stopping at the first failure has
-already run every other test."""
+already run every other test.  It is also pinned directly to the reference's
+own Hamiltonians (the probe_hvv fixtures written by the reference built from
+its sources), for MA and MAA."""
 import ctypes
 
 import numpy as np
 import pytest
 
 import xflat_gb300 as xg
-from helpers import derive
+from helpers import derive, golden, key
 
 pytestmark = pytest.mark.gpu
 
@@ -82,6 +84,28 @@ def test_static_entry_point_matches_xf_calc_hvv(base, over):
             second = _static_hvv(sim, cfg, pt, r, dr, dev)
             assert np.max(np.abs(first - ref)) <= tol
             assert np.max(np.abs(second - ref)) <= tol
+
+
+@pytest.mark.parametrize("name", ["ma_small_r10", "ma_c0shape", "maa_small_r10", "maa_ragged"])
+def test_static_entry_point_matches_reference_probes(name):
+    """phy::calc_Hvv of the reference at its three stage points, on the
+    reference's initial state, against the allocation-free entry point fed the
+    same state and this library's angle tables (which match the reference's to
+    2e-13)."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    g = golden(name)
+    cfg = xg.Config.from_text(g["config"])
+    sim = xg.Simulation(cfg)
+    sim.set_noise(g["meta"]["seed"], g["meta"]["noise_amp"])
+    r, dr = key(g["config"], "R0"), key(g["config"], "dr")
+    for pt in range(3):
+        ref = g["probe_hvv%d" % pt].reshape(-1, 4)
+        # the moment sums are reduced in a different order than the reference's serial loop
+        tol = 1e-12 * np.max(np.abs(ref))
+        for _ in range(2):
+            h = _static_hvv(sim, cfg, pt, r, dr, dev)
+            assert np.max(np.abs(h - ref)) <= tol, pt
 
 
 def test_static_entry_point_rejects_sizes_beyond_its_scratch():

@@ -14,7 +14,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "_lib")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU_SOURCES = ["xf_kernels.cu", "xf_engine.cu", "xf_mixed.cu", "xf_df.cu", "xf_batch.cu", "xf_probe.cu", "xf_noalloc.cu"]
+CU_SOURCES = ["xf_kernels.cu", "xf_engine.cu", "xf_mixed.cu", "xf_df.cu", "xf_persist.cu", "xf_batch.cu", "xf_probe.cu",
+              "xf_noalloc.cu"]
 CXX_SOURCES = ["xf_config.cpp", "xf_physics.cpp", "xf_netcdf.cpp", "xf_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

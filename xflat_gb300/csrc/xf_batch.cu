@@ -3,16 +3,18 @@
 //
 // Every instance keeps its own tables, state, control block and partial-sum
 // buffer (an xf_handle).  One iteration of the batch is one launch per stage
-// kernel over a work list of tiles: a tile is `warps` consecutive beams of one
-// instance, one warp per beam.  The blocks of an instance form that instance's
+// kernel over a work list of tiles: a tile is warps x beams-per-warp
+// consecutive beams of one instance, each warp striding over its beams.  The
+// blocks of an instance form that instance's
 // reduction group: the last of its tiles to finish reduces the instance's
 // moments in fixed order and, in the last phase, runs the instance's step
 // controller (accept/reject, dr, termination; src/Nmr.cpp:227-249).  An
 // instance that has finished skips its tiles, so instances with different step
 // counts share the launches.  Iterations are captured in CUDA graphs and the
 // host only polls a compact status array between graph launches.  The tile
-// shape (warps per tile) is chosen at creation by timing the candidates on the
-// batch itself (xf_batch_create's autotuner).
+// shape (warps per block, which sets the block size, and beams per warp,
+// which sets the number of blocks per phase) is chosen at creation by timing
+// the candidates on the batch itself (xf_batch_create's autotuner).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,6 +27,7 @@
 #include "xf_common.cuh"
 #include "xf_launch.cuh"
 #include "xf_engine.h"
+#include "xf_df.cuh"
 #include "xf_fp64.cuh"
 #include "xf_mixed.cuh"
 #include "xflat_gpu.h"
@@ -38,6 +41,7 @@ using namespace xf::detail;
 
 struct Tile {
     int inst, first, idx, count;  // instance, first beam, tile index and tile count within the instance
+    int end;                      // one past the tile's last beam
 };
 
 struct Status {
@@ -70,11 +74,14 @@ __global__ void __launch_bounds__(96) k_batch_geometry(const Dev* __restrict__ d
 }
 
 // The batched phases take the single-simulation kernels' register caps for
-// MA (resident warps per SM over spills; see xf_kernels.cu and xf_mixed.cu).
+// MA (resident warps per SM over spills; see xf_kernels.cu, xf_mixed.cu and
+// xf_df.cu).
 template <int PREC, int PH>
 constexpr int batch_min_blocks()
 {
-    return PREC == 0 ? (PH == xf::PH_C ? 3 : 1) : (PH == xf::PH_A ? 5 : (PH == xf::PH_B ? 6 : 4));
+    return PREC == XF_PREC_FP64    ? (PH == xf::PH_C ? 3 : 1)
+           : PREC == XF_PREC_MIXED ? (PH == xf::PH_A ? 5 : (PH == xf::PH_B ? 6 : 4))
+                                   : (PH == xf::PH_B ? 2 : 3);
 }
 
 template <int PREC, int PH>
@@ -85,14 +92,19 @@ __global__ void __launch_bounds__(256, batch_min_blocks<PREC, PH>()) k_batch_pha
     const Tile t = tiles[blockIdx.x];
     const Dev& d = devs[t.inst];
     const RedTarget rt = tile_target(d, t, PH);
-    if (PREC == 0) {
-        if (PH == xf::PH_A) xf::fp64::phaseA_body<0>(d, t.first, d.nbeams, rt);
-        else if (PH == xf::PH_B) xf::fp64::phaseB_body<0>(d, t.first, d.nbeams, rt);
-        else xf::fp64::phaseC_body<0>(d, t.first, d.nbeams, rt);
+    const int nw = blockDim.x >> 5;
+    if (PREC == XF_PREC_FP64) {
+        if (PH == xf::PH_A) xf::fp64::phaseA_body<0>(d, t.first, nw, rt, t.end);
+        else if (PH == xf::PH_B) xf::fp64::phaseB_body<0>(d, t.first, nw, rt, t.end);
+        else xf::fp64::phaseC_body<0>(d, t.first, nw, rt, t.end);
+    } else if (PREC == XF_PREC_MIXED) {
+        if (PH == xf::PH_A) xf::mixed::phaseA_body<0>(d, t.first, nw, rt, t.end);
+        else if (PH == xf::PH_B) xf::mixed::phaseB_body<0>(d, t.first, nw, rt, t.end);
+        else xf::mixed::phaseC_body<0>(d, t.first, nw, rt, t.end);
     } else {
-        if (PH == xf::PH_A) xf::mixed::phaseA_body<0>(d, t.first, d.nbeams, rt);
-        else if (PH == xf::PH_B) xf::mixed::phaseB_body<0>(d, t.first, d.nbeams, rt);
-        else xf::mixed::phaseC_body<0>(d, t.first, d.nbeams, rt);
+        if (PH == xf::PH_A) xf::dfp::phaseA_body<0>(d, t.first, nw, rt, t.end);
+        else if (PH == xf::PH_B) xf::dfp::phaseB_body<0>(d, t.first, nw, rt, t.end);
+        else xf::dfp::phaseC_body<0>(d, t.first, nw, rt, t.end);
     }
 }
 
@@ -102,7 +114,7 @@ __global__ void __launch_bounds__(256) k_batch_renorm(const Dev* __restrict__ de
 {
     xf::pdl_enter();
     const Tile t = tiles[blockIdx.x];
-    xf::mixed::esum_body(devs[t.inst], t.first, devs[t.inst].nbeams, 1, 1);
+    xf::mixed::esum_body(devs[t.inst], t.first, blockDim.x >> 5, 1, 1, t.end);
 }
 
 __global__ void __launch_bounds__(256) k_batch_moments(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
@@ -138,7 +150,8 @@ double now_s()
 struct xf_batch {
     std::vector<xf_handle*> h;
     int prec = XF_PREC_FP64;
-    int warps = 8;                  // beams per tile (= warps per block)
+    int warps = 8;                  // warps per block
+    int bpw = 1;                    // beams per warp (a tile holds warps x bpw beams)
     cudaStream_t st = nullptr;
     Dev* d_devs = nullptr;
     Tile* d_wtiles = nullptr;       // warp tiles for the stage kernels
@@ -154,7 +167,10 @@ struct xf_batch {
     };
     std::vector<G> graphs;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    double tuned_ms[3] = {0., 0., 0.};
+    static constexpr int kMaxCand = 16;
+    int ncand = 0;
+    int cand_warps[kMaxCand] = {}, cand_bpw[kMaxCand] = {};
+    double cand_ms[kMaxCand] = {};
     std::string err;
 
     int fail(int code, const std::string& m)
@@ -180,10 +196,11 @@ void drop_graphs(xf_batch* b)
 }
 
 // Work lists and per-instance device parameter blocks for a tile shape.
-int build_lists(xf_batch* b, int warps)
+int build_lists(xf_batch* b, int warps, int bpw)
 {
     drop_graphs(b);
     b->warps = warps;
+    b->bpw = bpw;
     const int n = (int)b->h.size();
     std::vector<Tile> wt, tt;
     std::vector<int2> ang;
@@ -192,10 +209,11 @@ int build_lists(xf_batch* b, int warps)
     size_t part_total = 0;
     for (int i = 0; i < n; ++i) {
         const xf_handle* h = b->h[i];
-        const int nwti = (h->nbeams + warps - 1) / warps;
+        const int span = warps * bpw;
+        const int nwti = (h->nbeams + span - 1) / span;
         const int ntti = (h->nbeams + 255) / 256;
-        for (int t = 0; t < nwti; ++t) wt.push_back(Tile{i, t * warps, t, nwti});
-        for (int t = 0; t < ntti; ++t) tt.push_back(Tile{i, t * 256, t, ntti});
+        for (int t = 0; t < nwti; ++t) wt.push_back(Tile{i, t * span, t, nwti, std::min(h->nbeams, (t + 1) * span)});
+        for (int t = 0; t < ntti; ++t) tt.push_back(Tile{i, t * 256, t, ntti, std::min(h->nbeams, (t + 1) * 256)});
         for (int a = 0; a < h->A; ++a) ang.push_back(make_int2(i, a));
         part_off[i] = part_total;
         if (std::max(nwti, ntti) > xf::kRedGroup * xf::kMaxRedGroups)
@@ -244,13 +262,17 @@ void launch_iteration(xf_batch* b)
     if (b->prec == XF_PREC_MIXED) {
         xf::launch_pdl(k_batch_renorm, b->nwt, threads, b->st, dv, wt);
         xf::launch_pdl(k_batch_moments, b->ntt, 256, b->st, dv, (const Tile*)b->d_ttiles);
-        xf::launch_pdl(k_batch_phase<1, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
-        xf::launch_pdl(k_batch_phase<1, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
-        xf::launch_pdl(k_batch_phase<1, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_MIXED, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_MIXED, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_MIXED, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
+    } else if (b->prec == XF_PREC_DF) {
+        xf::launch_pdl(k_batch_phase<XF_PREC_DF, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_DF, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_DF, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
     } else {
-        xf::launch_pdl(k_batch_phase<0, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
-        xf::launch_pdl(k_batch_phase<0, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
-        xf::launch_pdl(k_batch_phase<0, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_FP64, xf::PH_A>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_FP64, xf::PH_B>, b->nwt, threads, b->st, dv, wt);
+        xf::launch_pdl(k_batch_phase<XF_PREC_FP64, xf::PH_C>, b->nwt, threads, b->st, dv, wt);
     }
 }
 
@@ -337,8 +359,7 @@ int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out)
     if (!cfgs || n <= 0 || !out) return XF_EINVAL;
     *out = nullptr;
     for (int i = 0; i < n; ++i)
-        if ((cfgs[i].geometry != XF_GEOM_MA && cfgs[i].geometry != XF_GEOM_SA) || cfgs[i].precision != cfgs[0].precision ||
-            cfgs[i].precision == XF_PREC_DF)
+        if ((cfgs[i].geometry != XF_GEOM_MA && cfgs[i].geometry != XF_GEOM_SA) || cfgs[i].precision != cfgs[0].precision)
             return XF_EUNSUPPORTED;
     xf_batch* b = new xf_batch();
     b->prec = cfgs[0].precision;
@@ -353,23 +374,30 @@ int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out)
     if (rc == XF_OK && cudaMalloc(&b->d_status, n * sizeof(Status)) != cudaSuccess) rc = XF_ENOMEM;
     if (rc == XF_OK && cudaMallocHost(&b->h_status, n * sizeof(Status)) != cudaSuccess) rc = XF_ENOMEM;
     // autotune the tile shape on the batch itself: a few iterations per
-    // candidate from the initial states, which are restored afterwards
+    // candidate (warps per block x beams per warp) from the initial states,
+    // which are restored afterwards
     if (rc == XF_OK) {
-        const int cand[3] = {2, 4, 8};
+        const int cw[3] = {2, 4, 8}, cb[3] = {1, 2, 4};
         double best = 1e300;
-        int best_w = 8;
-        for (int c = 0; c < 3 && rc == XF_OK; ++c) {
-            rc = build_lists(b, cand[c]);
-            double ms = 0.;
-            if (rc == XF_OK) rc = run(b, 2, false, nullptr);      // first launch instantiates the graph
-            if (rc == XF_OK) rc = run(b, 8, false, &ms);
-            b->tuned_ms[c] = ms;
-            if (rc == XF_OK && ms < best) {
-                best = ms;
-                best_w = cand[c];
+        int best_w = 8, best_b = 1;
+        b->ncand = 0;
+        for (int i = 0; i < 3 && rc == XF_OK; ++i)
+            for (int j = 0; j < 3 && rc == XF_OK; ++j) {
+                rc = build_lists(b, cw[i], cb[j]);
+                double ms = 0.;
+                if (rc == XF_OK) rc = run(b, 2, false, nullptr);  // first launch instantiates the graph
+                if (rc == XF_OK) rc = run(b, 8, false, &ms);
+                const int c = b->ncand++;
+                b->cand_warps[c] = cw[i];
+                b->cand_bpw[c] = cb[j];
+                b->cand_ms[c] = ms;
+                if (rc == XF_OK && ms < best) {
+                    best = ms;
+                    best_w = cw[i];
+                    best_b = cb[j];
+                }
             }
-        }
-        if (rc == XF_OK) rc = build_lists(b, best_w);
+        if (rc == XF_OK) rc = build_lists(b, best_w, best_b);
         for (int i = 0; i < n && rc == XF_OK; ++i) {
             std::vector<double> psi;
             xf::initial_state(b->h[i]->nbeams, b->h[i]->ne, cfgs[i].seed, cfgs[i].noise_amp, psi);
@@ -449,8 +477,31 @@ int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms)
 {
     if (!b) return XF_EINVAL;
     if (warps) *warps = b->warps;
+    // the one-beam-per-warp candidates {2, 4, 8} warps
     if (tuned_ms)
-        for (int i = 0; i < 3; ++i) tuned_ms[i] = b->tuned_ms[i];
+        for (int i = 0, k = 0; i < b->ncand && k < 3; ++i)
+            if (b->cand_bpw[i] == 1) tuned_ms[k++] = b->cand_ms[i];
+    return XF_OK;
+}
+
+int xf_batch_set_shape(xf_batch* b, int warps, int beams_per_warp)
+{
+    if (!b || warps < 1 || warps > 8 || beams_per_warp < 1 || beams_per_warp > 64) return XF_EINVAL;
+    return build_lists(b, warps, beams_per_warp);
+}
+
+int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* ncand, int* cand_warps, int* cand_bpw,
+                    double* cand_ms)
+{
+    if (!b) return XF_EINVAL;
+    if (warps) *warps = b->warps;
+    if (beams_per_warp) *beams_per_warp = b->bpw;
+    if (ncand) *ncand = b->ncand;
+    for (int i = 0; i < b->ncand; ++i) {
+        if (cand_warps) cand_warps[i] = b->cand_warps[i];
+        if (cand_bpw) cand_bpw[i] = b->cand_bpw[i];
+        if (cand_ms) cand_ms[i] = b->cand_ms[i];
+    }
     return XF_OK;
 }
 

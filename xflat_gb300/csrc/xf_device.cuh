@@ -64,6 +64,8 @@ struct Ctl {
     float* m4hi;
     float* m4lo;
     unsigned int ticket[4];  // last-block tickets per phase
+    unsigned int bar;     // persistent loop: grid-barrier arrivals of the current launch
+    int bar_timeout;      // persistent loop: a barrier wait ran out
     int done;             // device control: no further iterations
     int nan_seen;
     long long iters;      // counter_tot

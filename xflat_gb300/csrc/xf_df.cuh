@@ -1,8 +1,8 @@
-// Double-float per-phase kernel bodies (MA and SA geometry): the FP64 path's
-// stages, with every state, propagator, average and moment carried as a pair
-// of FP32 numbers (hi + lo, about 48 significant bits) and computed with FP32
-// error-free transformations instead of on the FP64 pipe, which runs at 1/64
-// of the FP32 rate on this GPU.
+// Double-float per-phase kernel bodies (MA, MAA and SA geometry): the FP64
+// path's stages, with every state, propagator, average and moment carried as
+// a pair of FP32 numbers (hi + lo, about 48 significant bits) and computed
+// with FP32 error-free transformations instead of on the FP64 pipe, which runs
+// at 1/64 of the FP32 rate on this GPU.
 //
 // The stages, buffers and reductions are those of xf_fp64.cuh: phase A forms
 // psi1 = U(h0, dl1) psi0 (stored halved) and psi3 = U(h0, dl0) psi0 with their
@@ -18,13 +18,24 @@
 // C and S by less than 5e-15 (3.1e-15 at t = 1e-3), otherwise the series is
 // a pair Horner up to t = 0.25 and FP64 sincos beyond.
 //
-// The per-beam Hamiltonian offsets are formed in FP64 (two operations per
-// offset, once per beam) and split into pairs; the vacuum term, energy
-// weights and path lengths come from pair tables.  Moments are accumulated
-// in pairs, scaled by kappa (add_moment_df), and reduced across blocks in
-// FP64.  psi0 and the candidate share the mixed path's compensated-pair
-// buffers; psi1 and psi3 are pairs stored in the FP64 path's buffers
-// ([nbeams][4][epad] hi, then lo).
+// Arithmetic.  Intermediate values are "loose" pairs: the hi parts of
+// products and sums are exact error-free transformations (TwoProduct with
+// FMA, TwoSum), the lo parts collect the rounding errors and cross terms in
+// plain FP32, and a pair is renormalised (Fast2Sum) only where it is stored.
+// A lo part is then not necessarily below half an ulp of its hi part, but it
+// stays below about 2^-22 of the magnitudes of the operands that formed it,
+// so every value keeps an absolute error near 2^-47 of its natural scale (the
+// state is O(1), an increment |h| dl); stored states are renormalised and
+// exact to 2^-48.  The error-free steps use the _rn intrinsics, which the
+// compiler never contracts into FMAs.
+//
+// The per-beam Hamiltonian offsets are formed in FP64 (a few operations per
+// offset, once per beam, lane-parallel) and split into pairs; the vacuum
+// term, energy weights and path lengths come from pair tables.  Moments are
+// accumulated in pairs, scaled by kappa (add_moment_df), and reduced across
+// blocks in FP64.  psi0 and the candidate share the mixed path's
+// compensated-pair buffers; psi1 and psi3 are pairs stored in the FP64
+// path's buffers ([nbeams][4][epad] hi, then lo).
 #pragma once
 #include "xf_mixed.cuh"
 
@@ -35,12 +46,87 @@ using namespace detail;
 using mixed::DF;
 using mixed::df_add;
 using mixed::df_mul;
-using mixed::df_neg;
-using mixed::df_sub;
 using mixed::df_value;
-using mixed::fast_two_sum;
-using mixed::two_prod;
-using mixed::two_sum;
+
+// ------------------------------------------------------------------ loose pair arithmetic
+
+__device__ __forceinline__ DF two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return DF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ DF two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp))};
+}
+
+// Renormalisation (Fast2Sum): exact when |h| >= |l| or h = 0.
+__device__ __forceinline__ DF norm(const DF& a)
+{
+    const float s = __fadd_rn(a.h, a.l);
+    return DF{s, __fsub_rn(a.l, __fsub_rn(s, a.h))};
+}
+
+__device__ __forceinline__ DF neg(const DF& a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF dscale(float s, const DF& a) { return DF{s * a.h, s * a.l}; }  // s a power of two
+
+// a b (the lo*lo product, 2^-48 of the result, is dropped).
+__device__ __forceinline__ DF lmul(const DF& a, const DF& b)
+{
+    const DF p = two_prod(a.h, b.h);
+    return DF{p.h, fmaf(a.h, b.l, fmaf(a.l, b.h, p.l))};
+}
+
+// a a.
+__device__ __forceinline__ DF lsq(const DF& a)
+{
+    const DF p = two_prod(a.h, a.h);
+    return DF{p.h, fmaf(a.h + a.h, a.l, p.l)};
+}
+
+__device__ __forceinline__ DF ladd(const DF& a, const DF& b)
+{
+    const DF s = two_sum(a.h, b.h);
+    return DF{s.h, s.l + (a.l + b.l)};
+}
+
+__device__ __forceinline__ DF lsub(const DF& a, const DF& b) { return ladd(a, neg(b)); }
+
+// a + b for |a| >= |b| (Fast2Sum on the hi parts).
+__device__ __forceinline__ DF ladd_big(const DF& a, const DF& b)
+{
+    const float s = __fadd_rn(a.h, b.h);
+    return DF{s, __fsub_rn(b.h, __fsub_rn(s, a.h)) + (a.l + b.l)};
+}
+
+// a0 b0 + a1 b1.
+__device__ __forceinline__ DF ldot2(const DF& a0, const DF& b0, const DF& a1, const DF& b1)
+{
+    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h);
+    const DF s = two_sum(p.h, q.h);
+    const float lo = fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, p.l)) + fmaf(a1.h, b1.l, fmaf(a1.l, b1.h, q.l));
+    return DF{s.h, s.l + lo};
+}
+
+// a0 b0 + a1 b1 + a2 b2.
+__device__ __forceinline__ DF ldot3(const DF& a0, const DF& b0, const DF& a1, const DF& b1, const DF& a2, const DF& b2)
+{
+    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h), r = two_prod(a2.h, b2.h);
+    const DF s = two_sum(p.h, q.h);
+    const DF u = two_sum(s.h, r.h);
+    const float lo = fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, p.l)) + fmaf(a1.h, b1.l, fmaf(a1.l, b1.h, q.l)) +
+                     fmaf(a2.h, b2.l, fmaf(a2.l, b2.h, r.l));
+    return DF{u.h, (s.l + u.l) + lo};
+}
+
+__device__ __forceinline__ DF dsplit(double x)
+{
+    const float h = (float)x;
+    return DF{h, (float)(x - (double)h)};
+}
 
 struct DF4 {
     DF ar, ai, br, bi;
@@ -56,7 +142,18 @@ __device__ __forceinline__ DF4 load_df(const float* __restrict__ hi, const float
     return x;
 }
 
-__device__ __forceinline__ void store_df(float* __restrict__ hi, float* __restrict__ lo, int epad, int e, const DF4& x)
+__device__ __forceinline__ DF4 norm4(const DF4& x)
+{
+    DF4 y;
+    y.ar = norm(x.ar);
+    y.ai = norm(x.ai);
+    y.br = norm(x.br);
+    y.bi = norm(x.bi);
+    return y;
+}
+
+// Stores a renormalised x.
+__device__ __forceinline__ void store_raw(float* __restrict__ hi, float* __restrict__ lo, int epad, int e, const DF4& x)
 {
     hi[e] = x.ar.h;
     lo[e] = x.ar.l;
@@ -68,52 +165,35 @@ __device__ __forceinline__ void store_df(float* __restrict__ hi, float* __restri
     lo[3 * epad + e] = x.bi.l;
 }
 
-__device__ __forceinline__ DF dscale(float s, const DF& a) { return DF{s * a.h, s * a.l}; }  // s a power of two
-
-// a0 b0 + a1 b1 (the lo*lo products, 2^-48 of the terms, are dropped).
-__device__ __forceinline__ DF dot2(const DF& a0, const DF& b0, const DF& a1, const DF& b1)
+// Stores x renormalised.
+__device__ __forceinline__ void store_df(float* __restrict__ hi, float* __restrict__ lo, int epad, int e, const DF4& x)
 {
-    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h);
-    const DF s = two_sum(p.h, q.h);
-    const float cross = fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, fmaf(a1.h, b1.l, a1.l * b1.h)));
-    return fast_two_sum(s.h, s.l + ((p.l + q.l) + cross));
+    store_raw(hi, lo, epad, e, norm4(x));
 }
 
-// a0 b0 + a1 b1 + a2 b2.
-__device__ __forceinline__ DF dot3(const DF& a0, const DF& b0, const DF& a1, const DF& b1, const DF& a2, const DF& b2)
+__device__ __forceinline__ void prefetch_rows(const float* b, int epad, int e)
 {
-    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h), r = two_prod(a2.h, b2.h);
-    const DF s = two_sum(p.h, q.h);
-    const DF u = two_sum(s.h, r.h);
-    const float cross = fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, fmaf(a1.h, b1.l, fmaf(a1.l, b1.h, fmaf(a2.h, b2.l, a2.l * b2.h)))));
-    return fast_two_sum(u.h, (s.l + u.l) + ((p.l + q.l + r.l) + cross));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + e));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + epad + e));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + 2 * epad + e));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + 3 * epad + e));
 }
 
-__device__ __forceinline__ DF dsplit(double x)
-{
-    const float h = (float)x;
-    return DF{h, (float)(x - (double)h)};
-}
+// ------------------------------------------------------------------ propagators
 
 // Propagator coefficients: U = q + cm - i S sigma(h), cm = q (C - 1).
 struct DK {
     DF cm, S;
 };
 
-// Per-beam constants of a propagator: h01i^2 and dl^2 as pairs, and dl.
-struct DBeam {
-    DF h01i, h01i2, dl, dl2;
+// Per-beam constants of a propagator: the path length dl and dl^2, and the
+// square of the beam's h01i (pairs).
+struct DLen {
+    DF dl, dl2;
 };
 
-__device__ __forceinline__ DBeam dbeam(const DF& h01i, const DF& dl)
-{
-    DBeam b;
-    b.h01i = h01i;
-    b.h01i2 = df_mul(h01i, h01i);
-    b.dl = dl;
-    b.dl2 = df_mul(dl, dl);
-    return b;
-}
+__device__ __forceinline__ DLen dlen(const DF& dl) { return DLen{dl, norm(lsq(dl))}; }
+__device__ __forceinline__ DF dsq(const DF& h01i) { return norm(lsq(h01i)); }
 
 // c1 = (cos(sqrt t) - 1)/t and s1 = (sin(sqrt t)/sqrt t - 1)/t: the Taylor
 // coefficients from k = 1 on (c: (-1)^k / (2k)!, s: (-1)^k / (2k+1)!), each
@@ -129,37 +209,48 @@ __constant__ DConst kDS[7] = {XF_DFC(-1.0 / 6.0),         XF_DFC(1.0 / 120.0),  
                               XF_DFC(1.0 / 362880.0),     XF_DFC(-1.0 / 39916800.0),    XF_DFC(1.0 / 6227020800.0),
                               XF_DFC(-1.0 / 1307674368000.0)};
 #undef XF_DFC
+constexpr float kS1h = (float)(-1.0 / 6.0);
+constexpr float kS1l = (float)(-1.0 / 6.0 - (double)(float)(-1.0 / 6.0));
 
 __device__ __forceinline__ DF dconst(const DConst& c) { return DF{c.h, c.l}; }
 
 // Coefficients of U over dl for the bin Hamiltonian (h00, h01r, beam h01i).
 // Must be called by all 32 lanes of the warp (warp-uniform series choice).
 template <int Q2>
-__device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DBeam& bm)
+__device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DF& h01i2, const DLen& bm)
 {
     constexpr float q = Q2 ? 0.5f : 1.f;
-    const DF lam2 = df_add(dot2(h00, h00, h01r, h01r), bm.h01i2);
-    const DF t = df_mul(lam2, bm.dl2);
-    DF c1, s1;
-    bool direct = false;
+    const DF lam2 = ladd(ladd(lsq(h00), lsq(h01r)), h01i2);
+    const DF t = lmul(lam2, bm.dl2);
     DK k;
     if (__all_sync(kFull, t.h <= 1e-3f)) {
-        // tails t (1/24 - t/720) and t (1/120 - t/5040) in FP32: below 4.2e-5
-        // and 8.4e-6, rounded to 2^-24 of that and computed from t rounded to
-        // FP32; the next terms, t^3/40320 and t^3/362880, are below 2.5e-14
-        // and 2.8e-15 of c1 and s1; all of it enters C and S times t
+        // c1 = -1/2 + th (1/24 - th/720) and s1 = -1/6 + th (1/120 - th/5040):
+        // the tails are below 4.2e-5 and 8.4e-6, rounded to 2^-24 of that and
+        // computed from t rounded to FP32; the next terms, t^3/40320 and
+        // t^3/362880, are below 2.5e-14 and 2.8e-15 of c1 and s1; all of it
+        // enters C and S times t
         const float th = t.h;
-        c1 = fast_two_sum(-0.5f, th * fmaf(th, -1.f / 720.f, 1.f / 24.f));
-        s1 = df_add(dconst(kDS[0]), DF{th * fmaf(th, -1.f / 5040.f, 1.f / 120.f), 0.f});
+        const float ct = th * fmaf(th, -1.f / 720.f, 1.f / 24.f);
+        const float st = th * fmaf(th, -1.f / 5040.f, 1.f / 120.f);
+        // cm = q t c1 = -q t / 2 + q t ct, renormalised: its lo part (up to
+        // 8e-5 of the hi part before) enters FP32 products with the state
+        k.cm = norm(DF{-0.5f * q * t.h, fmaf(q * t.h, ct, q * fmaf(t.l, ct, -0.5f * t.l))});
+        // S = q dl (1 + t s1), |t s1| <= 1.7e-4; s1 = -1/6 + st renormalised
+        const DF s1 = two_sum(kS1h, st);
+        const DF u = lmul(t, DF{s1.h, s1.l + kS1l});
+        k.S = dscale(q, ladd_big(bm.dl, lmul(bm.dl, u)));
     } else if (t.h <= 0.25f) {
         // pair Horner to degree 7 in t (truncation below 1e-18 at t = 0.25)
-        c1 = dconst(kDC[6]);
-        s1 = dconst(kDS[6]);
+        const DF tn = norm(t);
+        DF c1 = dconst(kDC[6]), s1 = dconst(kDS[6]);
 #pragma unroll
         for (int i = 5; i >= 0; --i) {
-            c1 = df_add(dconst(kDC[i]), df_mul(c1, t));
-            s1 = df_add(dconst(kDS[i]), df_mul(s1, t));
+            c1 = df_add(dconst(kDC[i]), df_mul(c1, tn));
+            s1 = df_add(dconst(kDS[i]), df_mul(s1, tn));
         }
+        k.cm = dscale(q, df_mul(tn, c1));
+        const DF dl = norm(bm.dl);
+        k.S = dscale(q, df_add(dl, df_mul(dl, df_mul(tn, s1))));
     } else {
         const double lam = sqrt(df_value(lam2));
         const double dl = df_value(bm.dl);
@@ -167,11 +258,6 @@ __device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DBeam
         sincos(lam * dl, &sn, &cs);
         k.cm = dsplit(q * (cs - 1.0));
         k.S = dsplit(q * (sn / lam));
-        direct = true;
-    }
-    if (!direct) {
-        k.cm = dscale(q, df_mul(t, c1));
-        k.S = dscale(q, df_add(bm.dl, df_mul(bm.dl, df_mul(t, s1))));
     }
     return k;
 }
@@ -180,43 +266,44 @@ __device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DBeam
 __device__ __forceinline__ DF4 dsig_w(const DF& h00, const DF& h01r, const DF& h01i, const DF4& x)
 {
     DF4 w;
-    w.ar = dot3(h00, x.ai, h01i, x.br, h01r, x.bi);
-    w.ai = dot3(df_neg(h00), x.ar, h01i, x.bi, df_neg(h01r), x.br);
-    w.br = dot3(df_neg(h01i), x.ar, h01r, x.ai, df_neg(h00), x.bi);
-    w.bi = dot3(df_neg(h01i), x.ai, df_neg(h01r), x.ar, h00, x.br);
+    w.ar = ldot3(h00, x.ai, h01i, x.br, h01r, x.bi);
+    w.ai = ldot3(neg(h00), x.ar, h01i, x.bi, neg(h01r), x.br);
+    w.br = ldot3(neg(h01i), x.ar, h01r, x.ai, neg(h00), x.bi);
+    w.bi = ldot3(neg(h01i), x.ai, neg(h01r), x.ar, h00, x.br);
     return w;
 }
 
-// y = U x = q x + cm x + S w.
+// y = U x = q x + cm x + S w (loose; store_df renormalises).
 __device__ __forceinline__ DF4 dapply(float q, const DK& k, const DF4& x, const DF4& w)
 {
     DF4 y;
-    y.ar = df_add(dscale(q, x.ar), dot2(k.cm, x.ar, k.S, w.ar));
-    y.ai = df_add(dscale(q, x.ai), dot2(k.cm, x.ai, k.S, w.ai));
-    y.br = df_add(dscale(q, x.br), dot2(k.cm, x.br, k.S, w.br));
-    y.bi = df_add(dscale(q, x.bi), dot2(k.cm, x.bi, k.S, w.bi));
+    y.ar = ladd(dscale(q, x.ar), ldot2(k.cm, x.ar, k.S, w.ar));
+    y.ai = ladd(dscale(q, x.ai), ldot2(k.cm, x.ai, k.S, w.ai));
+    y.br = ladd(dscale(q, x.br), ldot2(k.cm, x.br, k.S, w.br));
+    y.bi = ladd(dscale(q, x.bi), ldot2(k.cm, x.bi, k.S, w.bi));
     return y;
 }
 
 __device__ __forceinline__ DF4 dadd4(const DF4& a, const DF4& b)
 {
     DF4 c;
-    c.ar = df_add(a.ar, b.ar);
-    c.ai = df_add(a.ai, b.ai);
-    c.br = df_add(a.br, b.br);
-    c.bi = df_add(a.bi, b.bi);
+    c.ar = ladd(a.ar, b.ar);
+    c.ai = ladd(a.ai, b.ai);
+    c.br = ladd(a.br, b.br);
+    c.bi = ladd(a.bi, b.bi);
     return c;
 }
 
 // Accumulates fv * rho(x) (acc_rho of xf_fp64.cuh: component 0 without the 1/2).
 __device__ __forceinline__ void dacc_rho(const DF4& x, const DF& fv, DF& s0, DF& s2, DF& s3)
 {
-    const DF d0 = df_sub(dot2(x.ar, x.ar, x.ai, x.ai), dot2(x.br, x.br, x.bi, x.bi));
-    const DF d2 = dot2(x.ar, x.br, x.ai, x.bi);
-    const DF d3 = dot2(x.ai, x.br, df_neg(x.ar), x.bi);
-    s0 = df_add(s0, df_mul(d0, fv));
-    s2 = df_add(s2, df_mul(d2, fv));
-    s3 = df_add(s3, df_mul(d3, fv));
+    const DF d0 = lsub(ladd(lsq(x.ar), lsq(x.ai)), ladd(lsq(x.br), lsq(x.bi)));
+    const DF d2 = ldot2(x.ar, x.br, x.ai, x.bi);
+    const DF d3 = ldot2(x.ai, x.br, neg(x.ar), x.bi);
+    // the sums stay normalised, so their lo parts round at 2^-48 of the sums
+    s0 = norm(ladd(s0, lmul(d0, fv)));
+    s2 = norm(ladd(s2, lmul(d2, fv)));
+    s3 = norm(ladd(s3, lmul(d3, fv)));
 }
 
 __device__ __forceinline__ DF shfl_df(const DF& v, int src)
@@ -234,6 +321,16 @@ __device__ __forceinline__ DF fv_df(const Dev& d, int p, int e)
     return DF{d.fvf[p * d.epad + e], d.fvf_lo[p * d.epad + e]};
 }
 
+// Per-beam sums of a warp, renormalised, then reduce-scattered (each group of
+// 32/NV lanes holds the warp total of one value).
+template <int NV>
+__device__ __forceinline__ void reduce_sums(DF (&v)[NV], int lane)
+{
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = norm(v[i]);
+    mixed::df_reduce_scatter<NV>(v, lane);
+}
+
 // psi1 / psi3 pair buffers inside the FP64 path's double buffers.
 __device__ __forceinline__ float* pair_hi(double* buf) { return reinterpret_cast<float*>(buf); }
 __device__ __forceinline__ size_t pair_span(const Dev& d) { return (size_t)d.nbeams * 4 * d.epad; }
@@ -241,9 +338,8 @@ __device__ __forceinline__ size_t pair_span(const Dev& d) { return (size_t)d.nbe
 // ------------------------------------------------------------------ phase A
 
 template <int GEOM>
-__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
-    static_assert(GEOM == 0, "the double-float path covers the MA and SA geometries");
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
     if (ctl->done) return;
@@ -260,29 +356,41 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     const int epad = d.epad;
     DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
     const int myv = lane >> 2;
+    const int pf = 32 * d.prefetch;
     const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         if (stage) stage_beam(d, ctl, stage, b, lane, nullptr, ctl->m0hi, ctl->m0lo);
-        // lane-parallel set-up: lanes 0-2 the offsets of H0 (FP64, split), lane 3 dl0
+        // lane-parallel set-up: lanes 0-2 the offsets of H0 (FP64, split), lanes 3-4 dl0, dl1
         DF sv{0.f, 0.f};
         if (lane < 3) sv = dsplit(beam_offset_k<GEOM>(d, ctl->J0, 0, hm, bi, lane));
-        else if (lane == 3) sv = mixed::dfg(d, 3, 0, bi.ang);
-        const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2), dl0 = shfl_df(sv, 3);
-        const DBeam bm = dbeam(g01i, dl0);
+        else if (lane < 5) sv = mixed::dfg(d, 3, lane - 3, bi.ang);
+        const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2);
+        const DF g01i2 = dsq(g01i);
+        const DLen bm0 = dlen(shfl_df(sv, 3));
+        DLen bm1;
+        if (GEOM == 1) bm1 = dlen(shfl_df(sv, 4));
         const size_t base = (size_t)b * 4 * epad;
         DF v[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) v[i] = DF{0.f, 0.f};
         for (int e = lane; e < epad; e += 32) {
-            const DF a00 = df_add(hv_df(d, 0, e), g00), a01 = df_add(hv_df(d, 1, e), g01r);
+            if (pf && e + pf < epad) {
+                prefetch_rows(h0 + base, epad, e + pf);
+                prefetch_rows(l0 + base, epad, e + pf);
+            }
+            const DF a00 = ladd(hv_df(d, 0, e), g00), a01 = ladd(hv_df(d, 1, e), g01r);
             const DF4 x = load_df(h0 + base, l0 + base, epad, e);
-            const DK k0 = dcoeffs<0>(a00, a01, bm);
-            // MA: dl1 = 2 dl0, so the halved U(dl1) has C1/2 - 1/2 = C0^2 - 1 =
-            // cm0 (2 + cm0) and S1/2 = C0 S0 = S0 + cm0 S0
+            const DK k0 = dcoeffs<0>(a00, a01, g01i2, bm0);
             DK k1;
-            k1.cm = df_mul(k0.cm, df_add(DF{2.f, 0.f}, k0.cm));
-            k1.S = df_add(k0.S, df_mul(k0.cm, k0.S));
+            if (GEOM == 0) {
+                // MA: dl1 = 2 dl0, so the halved U(dl1) has C1/2 - 1/2 = C0^2 - 1 =
+                // cm0 (2 + cm0) and S1/2 = C0 S0 = S0 + cm0 S0
+                k1.cm = lmul(k0.cm, ladd_big(DF{2.f, 0.f}, k0.cm));
+                k1.S = ladd_big(k0.S, lmul(k0.cm, k0.S));
+            } else {
+                k1 = dcoeffs<1>(a00, a01, g01i2, bm1);
+            }
             const DF4 w = dsig_w(a00, a01, g01i, x);
             const DF4 y1 = dapply(.5f, k1, x, w);
             const DF4 y3 = dapply(1.f, k0, x, w);
@@ -297,7 +405,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         v[1] = dscale(4.f, v[1]);
         v[2] = dscale(4.f, v[2]);
         v[3] = dscale(.5f, v[3]);
-        mixed::df_reduce_scatter<8>(v, lane);
+        reduce_sums<8>(v, lane);
         if (myv < 3) mixed::add_moment_df<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 3, acc);
         else if (myv < 6) mixed::add_moment_df<GEOM>(d, v[0], comp_of(myv - 3), 1, bi, lane & 3, acc);
     }
@@ -318,9 +426,8 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 // ------------------------------------------------------------------ phase B
 
 template <int GEOM>
-__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
-    static_assert(GEOM == 0, "the double-float path covers the MA and SA geometries");
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
     if (ctl->done) return;
@@ -338,7 +445,8 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int epad = d.epad;
     DF acc{0.f, 0.f};
     const int myv = lane >> 3;
-    for (int b = gw; b < d.nbeams; b += tw) {
+    const int pf = 32 * d.prefetch;
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up: lanes 0-2 the offsets of H1, 3-5 those of H3, lane 6 dl1
         DF sv{0.f, 0.f};
@@ -347,22 +455,28 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         else if (lane == 6) sv = mixed::dfg(d, 3, 1, bi.ang);
         const DF g100 = shfl_df(sv, 0), g101r = shfl_df(sv, 1), g101i = shfl_df(sv, 2);
         const DF g300 = shfl_df(sv, 3), g301r = shfl_df(sv, 4), g301i = shfl_df(sv, 5);
-        const DF dl1 = shfl_df(sv, 6);
-        const DBeam ba = dbeam(g101i, dl1), bb = dbeam(g301i, dl1);
+        const DLen bl = dlen(shfl_df(sv, 6));
+        const DF ga2 = dsq(g101i), gb2 = dsq(g301i);
         const size_t base = (size_t)b * 4 * epad;
         DF v[4] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
         for (int e = lane; e < epad; e += 32) {
+            if (pf && e + pf < epad) {
+                prefetch_rows(h0 + base, epad, e + pf);
+                prefetch_rows(l0 + base, epad, e + pf);
+                prefetch_rows(p1h + base, epad, e + pf);
+                prefetch_rows(p1h + span + base, epad, e + pf);
+            }
             const DF hv0 = hv_df(d, 0, e), hv1 = hv_df(d, 1, e);
             const DF4 x = load_df(h0 + base, l0 + base, epad, e);
             // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
-            const DF a00 = df_add(hv0, g100), a01 = df_add(hv1, g101r);
-            const DK ka = dcoeffs<1>(a00, a01, ba);
+            const DF a00 = ladd(hv0, g100), a01 = ladd(hv1, g101r);
+            const DK ka = dcoeffs<1>(a00, a01, ga2, bl);
             const DF4 ya = dapply(.5f, ka, x, dsig_w(a00, a01, g101i, x));
             const DF4 p1 = load_df(p1h + base, p1h + span + base, epad, e);
             store_df(p1h + base, p1h + span + base, epad, e, dadd4(ya, p1));
             // S8, stored halved for the average of S10/S11
-            const DF b00 = df_add(hv0, g300), b01 = df_add(hv1, g301r);
-            const DK kb = dcoeffs<1>(b00, b01, bb);
+            const DF b00 = ladd(hv0, g300), b01 = ladd(hv1, g301r);
+            const DK kb = dcoeffs<1>(b00, b01, gb2, bl);
             const DF4 y4 = dapply(.5f, kb, x, dsig_w(b00, b01, g301i, x));
             store_df(h4 + base, l4 + base, epad, e, y4);
             dacc_rho(y4, fv_df(d, bi.p, e), v[0], v[1], v[2]);
@@ -371,7 +485,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         v[0] = dscale(2.f, v[0]);
         v[1] = dscale(4.f, v[1]);
         v[2] = dscale(4.f, v[2]);
-        mixed::df_reduce_scatter<4>(v, lane);
+        reduce_sums<4>(v, lane);
         if (myv < 3) mixed::add_moment_df<GEOM>(d, v[0], comp_of(myv), 2, bi, lane & 7, acc);
     }
     if (!group_reduce_split<K>(rt, 8, 3, df_value(acc), 0., false, s_warp, s_out)) return;
@@ -386,9 +500,8 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
 // ------------------------------------------------------------------ phase C
 
 template <int GEOM>
-__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
-    static_assert(GEOM == 0, "the double-float path covers the MA and SA geometries");
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
     if (ctl->done) return;
@@ -408,37 +521,48 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     DF acc{0.f, 0.f};
     float mx = -1.f;
     const int myv = lane >> 3;  // 0: error, 1..3: density components 0, 2, 3
-    for (int b = gw; b < d.nbeams; b += tw) {
+    const int pf = 32 * d.prefetch;
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up: lanes 0-2 the offsets of H4, lane 3 dl2
         DF sv{0.f, 0.f};
         if (lane < 3) sv = dsplit(beam_offset_k<GEOM>(d, ctl->JB4, 2, hm_rdr, bi, lane));
         else if (lane == 3) sv = mixed::dfg(d, 3, 2, bi.ang);
-        const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2), dl2 = shfl_df(sv, 3);
-        const DBeam bm = dbeam(g01i, dl2);
+        const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2);
+        const DLen bm = dlen(shfl_df(sv, 3));
+        const DF g01i2 = dsq(g01i);
         const size_t base = (size_t)b * 4 * epad;
         DF v[4] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
         float err = 0.f;
         for (int e = lane; e < epad; e += 32) {
-            const DF a00 = df_add(hv_df(d, 0, e), g00), a01 = df_add(hv_df(d, 1, e), g01r);
+            if (pf && e + pf < epad) {
+                prefetch_rows(p3h + base, epad, e + pf);
+                prefetch_rows(p3h + span + base, epad, e + pf);
+                prefetch_rows(h4 + base, epad, e + pf);
+                prefetch_rows(l4 + base, epad, e + pf);
+                prefetch_rows(p1h + base, epad, e + pf);
+                prefetch_rows(p1h + span + base, epad, e + pf);
+            }
+            const DF a00 = ladd(hv_df(d, 0, e), g00), a01 = ladd(hv_df(d, 1, e), g01r);
             const DF4 x3 = load_df(p3h + base, p3h + span + base, epad, e);
             // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
-            const DK k = dcoeffs<1>(a00, a01, bm);
+            const DK k = dcoeffs<1>(a00, a01, g01i2, bm);
             const DF4 y3 = dapply(.5f, k, x3, dsig_w(a00, a01, g01i, x3));
-            const DF4 c = dadd4(y3, load_df(h4 + base, l4 + base, epad, e));
-            store_df(h4 + base, l4 + base, epad, e, c);
-            // calcErrHvv against psi1: the difference of two pairs is exact to
-            // 2^-48 of the state, far below the error's own size
+            const DF4 c = norm4(dadd4(y3, load_df(h4 + base, l4 + base, epad, e)));
+            store_raw(h4 + base, l4 + base, epad, e, c);
+            // calcErrHvv against psi1: the hi parts of two states this close
+            // differ exactly (Sterbenz), so the difference is exact to 2^-48
+            // of the state, far below the error's own size
             const DF4 r1 = load_df(p1h + base, p1h + span + base, epad, e);
-            const float e0 = df_sub(c.ar, r1.ar).h, e1 = df_sub(c.ai, r1.ai).h;
-            const float e2 = df_sub(c.br, r1.br).h, e3 = df_sub(c.bi, r1.bi).h;
+            const float e0 = (c.ar.h - r1.ar.h) + (c.ar.l - r1.ar.l), e1 = (c.ai.h - r1.ai.h) + (c.ai.l - r1.ai.l);
+            const float e2 = (c.br.h - r1.br.h) + (c.br.l - r1.br.l), e3 = (c.bi.h - r1.bi.h) + (c.bi.l - r1.bi.l);
             const DF f = fv_df(d, bi.p, e);
             err = fmaf((e0 * e0 + e1 * e1) + (e2 * e2 + e3 * e3), f.h, err);
             dacc_rho(c, f, v[1], v[2], v[3]);
         }
         v[0] = DF{err, 0.f};
         v[1] = dscale(.5f, v[1]);
-        mixed::df_reduce_scatter<4>(v, lane);
+        reduce_sums<4>(v, lane);
         if (myv == 0) {
             mx = fmaxf(mx, v[0].h + v[0].l);
             if ((lane & 7) == 0) {

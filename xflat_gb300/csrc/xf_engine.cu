@@ -49,10 +49,6 @@ int check_config(const xf_config& c, std::string& why)
         why = "precision must be fp64, mixed or df";
         return XF_EINVAL;
     }
-    if (c.precision == XF_PREC_DF && c.geometry == XF_GEOM_MAA) {
-        why = "the double-float path covers the MA and SA geometries";
-        return XF_EUNSUPPORTED;
-    }
     if (c.flvs != 2) { why = "only two flavors are supported (Flvs= 2), as by the MA/MAA modules"; return XF_EUNSUPPORTED; }
     if ((c.geometry != XF_GEOM_SA && c.abins <= 0) || c.ebins <= 0) { why = "Abins and Ebins must be positive"; return XF_EINVAL; }
     if (c.geometry == XF_GEOM_MAA && c.pbins <= 0) { why = "Pbins must be positive for MAA"; return XF_EINVAL; }
@@ -105,7 +101,10 @@ int xf_handle::init(const xf_config& c)
     epad = (ne + 31) / 32 * 32;
     nbeams = A * P * 4;
     shape = xf::default_shape(nbeams, epad, cfg.precision == XF_PREC_MIXED);
-    if (cfg.precision == XF_PREC_DF) renorm_every = 0;  // pair arithmetic keeps |a|^2 + |b|^2 = 1 to 2^-48
+    if (cfg.precision == XF_PREC_DF) {
+        renorm_every = 0;  // pair arithmetic keeps |a|^2 + |b|^2 = 1 to 2^-48
+        xf::df_default_shape(nbeams, shape);
+    }
     XF_CUDA(this, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     for (int i = 0; i < 7; ++i) XF_CUDA(this, cudaEventCreate(&ev[i]));
 
@@ -505,6 +504,36 @@ int xf_handle::get_graph(int k, bool timed, cudaGraphExec_t* out)
     return XF_OK;
 }
 
+// One cooperative launch of up to k device-controlled iterations (the
+// persistent loop, xf_persist.cu) followed by the copy of the control block,
+// as one launch of a k-iteration graph does.  A barrier wait that ran out
+// leaves the reduction tickets of an unfinished phase behind: they are
+// cleared, and the call reports XF_ETIMEOUT.
+int xf_handle::launch_persistent(int k)
+{
+    Dev d = dev;
+    d.device_control = 1;
+    d.log = d_log;
+    d.log_cap = log_cap_dev;
+    d.renorm_every = 0;
+    const int blocks = xf::persist_blocks(d);
+    if (blocks <= 0) return fail(XF_ECUDA, "persistent loop: the kernel cannot be resident");
+    XF_CUDA(this, cudaMemsetAsync(&d_ctl->bar, 0, sizeof(unsigned int), st));
+    const unsigned long long limit = (unsigned long long)(barrier_timeout_ms * 1e6);
+    XF_CUDA(this, xf::launch_persist(d, blocks, k, (unsigned)barrier_extra, limit, st));
+    XF_CUDA(this, cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    XF_CUDA(this, cudaStreamSynchronize(st));
+    if (h_ctl->bar_timeout) {
+        XF_CUDA(this, cudaMemsetAsync(d_gticket, 0, 4 * (size_t)xf::kMaxRedGroups * sizeof(unsigned int), st));
+        XF_CUDA(this, cudaMemsetAsync(&d_ctl->ticket[0], 0, sizeof(h_ctl->ticket), st));
+        XF_CUDA(this, cudaMemsetAsync(&d_ctl->bar_timeout, 0, sizeof(int), st));
+        XF_CUDA(this, cudaStreamSynchronize(st));
+        j0_valid = false;
+        return fail(XF_ETIMEOUT, "persistent loop: a grid-barrier wait ran out");
+    }
+    return XF_OK;
+}
+
 // Prepares the control block for a device-controlled loop from (r, dr) with
 // an iteration budget Ts: moments of psi0 at stage point 0 of r, counters
 // reset, done set if there is nothing to do.  Synchronous.
@@ -528,6 +557,8 @@ int xf_handle::start_device_run(double r, double dr, long Ts, bool files)
     h_ctl->renorm_due = 0;
     h_ctl->done = (r < cfg.Rn && Ts > 0) ? 0 : 1;
     for (int i = 0; i < 4; ++i) h_ctl->ticket[i] = 0;
+    h_ctl->bar = 0;
+    h_ctl->bar_timeout = 0;
     h_ctl->io_mode = 0;
     h_ctl->stage_kind = 0;
     if (files) io_dev_fill(h_ctl);
@@ -555,10 +586,12 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         log_cap_dev = o.log_cap;
     }
     const bool files = o.write_files && cfg.dump_mode != 0;
+    // the persistent loop serves FP64 and double-float; per-phase timing needs the graphs' events
+    const bool pers = persistent && (!mixed || dev.df) && !o.time_phases;
     if (files && (rc = io_dev_prepare(k))) return rc;
     if ((rc = start_device_run(r, dr, Ts, files))) return rc;
     // instantiate the graph sizes this run needs before the timed region starts
-    {
+    if (!pers) {
         cudaGraphExec_t ex;
         if (Ts > 0 && (rc = get_graph((int)std::min<long>(k, Ts), o.time_phases != 0, &ex))) return rc;
         if (Ts > k && Ts % k && (rc = get_graph((int)(Ts % k), o.time_phases != 0, &ex))) return rc;
@@ -574,22 +607,29 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         // graph node runs only to find the loop finished
         const long long left = Ts - prev_iters;
         const int kk = (int)std::min<long long>(k, std::max<long long>(1, left));
-        cudaGraphExec_t ex;
-        if ((rc = get_graph(kk, o.time_phases != 0, &ex))) return rc;
+        cudaGraphExec_t ex = nullptr;
+        if (!pers && (rc = get_graph(kk, o.time_phases != 0, &ex))) return rc;
         // every iteration of the launch may decide an output record: their slots must be free
         if (files && (rc = io_dev_reserve(kk))) return rc;
-        XF_CUDA(this, cudaGraphLaunch(ex, st));
-        // the previous launch's records go to the writer while this launch runs
-        if (io_pending && (rc = io_dev_drain(io_count, io_staged, false))) return rc;
-        io_pending = false;
-        XF_CUDA(this, cudaStreamSynchronize(st));
+        if (pers) {
+            // the previous launch's records go to the writer before this one
+            if (io_pending && (rc = io_dev_drain(io_count, io_staged, false))) return rc;
+            io_pending = false;
+            if ((rc = launch_persistent(kk))) return rc;
+        } else {
+            XF_CUDA(this, cudaGraphLaunch(ex, st));
+            // the previous launch's records go to the writer while this launch runs
+            if (io_pending && (rc = io_dev_drain(io_count, io_staged, false))) return rc;
+            io_pending = false;
+            XF_CUDA(this, cudaStreamSynchronize(st));
+        }
         if (files) {
             io_count = h_ctl->io_count;
             io_staged = h_ctl->io_staged;
             io_pending = true;
         }
         const long long ran = h_ctl->iters - prev_iters;
-        launches += 4 * ran;
+        launches += pers ? 1 : 4 * ran;
         d2h_bytes += sizeof(Ctl);  // the graph's copy of the control block
         if (o.time_phases) {
             for (long long i = 0; i < ran && i < kk; ++i)
@@ -715,13 +755,31 @@ int xf_set_option(xf_handle* h, const char* name, double value)
         const int cap = xf::max_phase_blocks(h->nbeams, 32);
         h->shape.blocks = std::min(h->shape.blocks, std::max(1, cap));
         h->shape.blocks_ab = std::min(h->shape.blocks_ab, std::max(1, cap));
+        for (int& pb : h->shape.phase_blocks) pb = std::min(pb, std::max(1, cap));
     } else if (n == "blocks") {
         const int b = (int)value;
         const int cap = std::max(xf::max_phase_blocks(h->nbeams, 256), 152 * 4);
         if (b < 0 || b > cap) return h->fail(XF_EINVAL, "blocks out of range");
-        const xf::Shape def = xf::default_shape(h->nbeams, h->epad, h->mixed != nullptr && !h->dev.df);
+        xf::Shape def = h->shape;
+        if (h->dev.df) xf::df_default_shape(h->nbeams, def);
+        else def = xf::default_shape(h->nbeams, h->epad, h->mixed != nullptr);
         h->shape.blocks = b ? b : def.blocks;
         h->shape.blocks_ab = b ? b : def.blocks_ab;
+        for (int p = 0; p < 3; ++p) h->shape.phase_blocks[p] = b ? b : def.phase_blocks[p];
+    } else if (n == "persistent") {
+        h->persistent = value != 0.;
+    } else if (n == "barrier_timeout_ms") {
+        if (!(value > 0.) || value > 60000.) return h->fail(XF_EINVAL, "barrier_timeout_ms must be in (0, 60000]");
+        h->barrier_timeout_ms = value;
+    } else if (n == "debug_barrier_extra") {
+        if (value < 0. || value > 1024.) return h->fail(XF_EINVAL, "debug_barrier_extra must be in [0, 1024]");
+        h->barrier_extra = (int)value;
+    } else if (n == "df_b_occupancy") {
+        const int o = (int)value;
+        if (!h->dev.df) return h->fail(XF_EUNSUPPORTED, "df_b_occupancy applies to the double-float path");
+        if (o != 2 && o != 3) return h->fail(XF_EINVAL, "df_b_occupancy must be 2 or 3");
+        h->shape.df_b_occ = o;
+        xf::df_default_shape(h->nbeams, h->shape);
     } else {
         return h->fail(XF_EINVAL, "unknown option " + n);
     }

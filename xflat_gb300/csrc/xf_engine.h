@@ -60,6 +60,9 @@ struct xf_handle {
     int renorm_every = 16;        // mixed precision: accepted steps between renormalisations
     int accepts_since_renorm = 0;
     int time_phases = 0;
+    int persistent = 0;           // device control as one cooperative launch per k iterations (FP64, df)
+    double barrier_timeout_ms = 2000.;  // limit of each grid-barrier wait of the persistent loop
+    int barrier_extra = 0;        // test hook: arrivals each barrier waits for beyond the grid (never come)
     double phase_ms[3] = {0., 0., 0.};
     long phase_n[3] = {0, 0, 0};
     long launches = 0;
@@ -89,6 +92,7 @@ struct xf_handle {
     int run_device(const xf_run_opts& o, xf_run_stats& s);
     int start_device_run(double r, double dr, long Ts, bool files = false);
     int get_graph(int k, bool timed, cudaGraphExec_t* out);
+    int launch_persistent(int k);
     int dump_files(long itr, double r, double dr);
     int flush_files();  // waits until every queued output record is written
     // Device-controlled runs with files (xf_io.cpp): slots and files before the

@@ -174,7 +174,7 @@ __device__ __forceinline__ void store_psi(double* __restrict__ base, int epad, i
 // S1 (H of psi0 from the cached moments), S2 and S6 (two sweeps sharing H0),
 // and the moments of psi1 at point 2 (S3) and of psi3 at point 1 (S7).
 template <int GEOM>
-__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
@@ -189,7 +189,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     const int myv = lane >> 2;  // value slot owned after an 8-way reduce-scatter
     const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         if (stage) stage_beam(d, ctl, stage, b, lane, psi0, nullptr, nullptr);
         // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
@@ -259,7 +259,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 // S4/S5 (psi4' = U(h1, dl1, hm(r+dr)) psi0 averaged into psi1) and S8
 // (psi4 = U(h3, dl1, hm(r+dr/2)) psi0) with the moments of psi4 at point 2 (S9).
 template <int GEOM>
-__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
@@ -274,7 +274,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int epad = d.epad;
     double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     const int myv = lane >> 3;
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up: lanes 0-2 the offsets of H1, 3-5 those of H3, lane 6 dl1
         double sv = 0.;
@@ -335,7 +335,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
 // Under device control the last block also runs the step controller of
 // src/Nmr.cpp:227-249.
 template <int GEOM>
-__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
@@ -351,7 +351,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     double acc = 0.;  // lane-split moment accumulator (add_moment_lane)
     double mx = -1.0;
     const int myv = lane >> 3;  // 0: error, 1..3: density components 0, 2, 3
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up: lanes 0-2 the offsets of H4, lane 3 dl2
         double sv = 0.;

@@ -458,7 +458,7 @@ __device__ __forceinline__ DF s0_df(const Ctl* ctl, int b, int comp)
 
 // Moments of psi1 = U(h0, dl1) psi0 at point 2 and of psi3 = U(h0, dl0) psi0 at point 1.
 template <int GEOM>
-__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseA_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
@@ -474,7 +474,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
     const int myv = lane >> 2;
     const int stage = ctl->stage_kind;  // an output record waits for psi0 (device control with files)
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         if (stage) stage_beam(d, ctl, stage, b, lane, nullptr, ctl->m0hi, ctl->m0lo);
         // lane-parallel set-up: lanes 0-2 the offsets of H0, lanes 3-4 dl0, dl1
@@ -545,7 +545,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 
 // Moments of psi4 = U(h3, dl1) psi0 at point 2.
 template <int GEOM>
-__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
@@ -560,7 +560,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const int epad = d.epad;
     DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
     const int myv = lane >> 3;
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up: lanes 0-2 the offsets of H3, lane 3 dl1
         float sv = 0.f;
@@ -631,7 +631,7 @@ __device__ __forceinline__ void c_bin(const H3f& h0, const H3f& h1, const H3f& h
 // d3' = d3 + K(h4,l2)(psi0 + d3), d4m = K(h3,l1) psi0; the error estimate in
 // difference form; moments of the candidate; the step controller.
 template <int GEOM>
-__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt)
+__device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
     Ctl* ctl = d.ctl;
@@ -652,7 +652,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     DF acc{0.f, 0.f};  // lane-split moment accumulator (add_moment_df)
     float mx = -1.f;
     const int myv = lane >> 3;
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         const BeamIdx bi = decode_beam(d, b);
         // lane-parallel set-up, one scalar per lane: offsets of H0, H1, H3, H4
         // (lanes 0-11), the differences H3 - H1 and H4 - H0 in FP64 (12-17),
@@ -799,7 +799,7 @@ __device__ __forceinline__ void renorm_bin_fp64(float* ph, float* pl, int epad, 
     }
 }
 
-__device__ inline void esum_body(const Dev& d, int first, int stride, int renorm, int conditional)
+__device__ inline void esum_body(const Dev& d, int first, int stride, int renorm, int conditional, int end = -1)
 {
     Ctl* ctl = d.ctl;
     if (conditional && !ctl->renorm_due) return;
@@ -809,7 +809,7 @@ __device__ inline void esum_body(const Dev& d, int first, int stride, int renorm
     float* hi = ctl->m0hi;
     float* lo = ctl->m0lo;
     double* S = ctl->S0;
-    for (int b = gw; b < d.nbeams; b += tw) {
+    for (int b = gw; b < (end < 0 ? d.nbeams : end); b += tw) {
         float* ph = hi + (size_t)b * 4 * epad;
         float* pl = lo + (size_t)b * 4 * epad;
         double v[4] = {0., 0., 0., 0.};

@@ -20,7 +20,12 @@
 //    that first call before any stream capture begins;
 //  * every call shares the one array and it keeps the last call's contents:
 //    each call clears the ticket it needs at zero, and calls that overlap on
-//    the GPU (different streams or threads, without ordering) race on it.
+//    the GPU (different streams or threads, without ordering) race on it;
+//  * `stream` must belong to the current device (XF_EINVAL otherwise), since
+//    the array's address is the current device's;
+//  * a CUDA error already pending when the call starts (left by the caller's
+//    own work) is reported as XF_ECUDA and left pending for the caller; a
+//    launch that fails is reported at once, before the next one is queued.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -213,10 +218,22 @@ extern "C" int xf_calc_hvv_static(int geometry, int abins, int pbins, int ebins,
     }
     if (!psi || !fv || !cosb || !dcosb || !LE || !hvv) return XF_EINVAL;
     if (geometry == XF_GEOM_MAA && (!sinb || !cosphi || !sinphi)) return XF_EINVAL;
+    // an error left by earlier work stays the caller's to see
+    if (cudaPeekAtLastError() != cudaSuccess) return XF_ECUDA;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int cur = -1, sdev = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) return XF_ECUDA;
+    if (st) {
+        if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) return XF_EINVAL;
+        if (sdev != cur) {
+            std::fprintf(stderr, "xf_calc_hvv_static: the stream belongs to device %d, the current device is %d\n",
+                         sdev, cur);
+            return XF_EINVAL;
+        }
+    }
     double* scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     StaticArgs a;
     a.geom = geometry;
     a.A = abins;
@@ -241,9 +258,11 @@ extern "C" int xf_calc_hvv_static(int geometry, int abins, int pbins, int ebins,
     int eb = (int)((nbeams + warps - 1) / warps);
     if (eb > 4096) eb = 4096;
     k_static_esum<<<eb, kThreads, 0, st>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return XF_ECUDA;
     int mb = (int)((nbeams + kThreads - 1) / kThreads);
     if (mb > kBlocks) mb = kBlocks;
     k_static_moments<<<mb, kThreads, 0, st>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return XF_ECUDA;
     const int nh = abins * P;
     k_static_hvv<<<(nh + 127) / 128, 128, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? XF_OK : XF_ECUDA;
