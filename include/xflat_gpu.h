@@ -147,7 +147,7 @@ int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins)
  * (default 16, 0 = never; the double-float path takes 0 only); "prefetch"
  * sets how many energy-loop iterations ahead the mixed and double-float phase
  * kernels prefetch the state rows into L1 (default 1, 0 = none);
- * "df_b_occupancy" (2 or 3, default 3) picks the double-float phase-B kernel
+ * "df_b_occupancy" (2 or 3, default 2) picks the double-float phase-B kernel
  * built for that many resident blocks per SM; "debug_psi3" = 1 makes the last
  * phase also store U(h4, dl2) psi3 into psi3, as the reference's in-place
  * stage S10 does (src/Nmr.cpp:191). */
@@ -283,6 +283,12 @@ int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* nca
 /* Replaces the tuned tile shape: warps per block in [1, 8], beams per warp in
  * [1, 64]. */
 int xf_batch_set_shape(xf_batch* b, int warps, int beams_per_warp);
+/* on = 1: run the batch's iterations as one cooperative launch per 8
+ * iterations (FP64 and df), the stages separated by grid barriers whose waits
+ * are bounded (XF_ETIMEOUT when one runs out), over 8-warp tiles of
+ * beams_per_warp beams per warp; on = 0: CUDA graphs of the per-stage
+ * launches (the default). */
+int xf_batch_set_persistent(xf_batch* b, int on, int beams_per_warp);
 
 #ifdef __cplusplus
 }

@@ -121,3 +121,24 @@ def test_batch_df_vs_fp64():
         a, c = b64.get_state(i), b2.get_state(i)
         pee = lambda x: x[0::4, 0] ** 2 + x[0::4, 1] ** 2
         assert np.max(np.abs(pee(a) - pee(c))) <= 1e-8
+
+
+@pytest.mark.parametrize("prec,bpw", [("fp64", 1), ("df", 2)])
+def test_batch_persistent_equals_graphs(prec, bpw):
+    """The batch as one cooperative launch per 8 iterations (grid barriers
+    between the stages) against the per-stage graph launches with the same
+    tile shape: the same decisions and states bit for bit."""
+    texts = _small_sweep(prec)
+    a = xg.Batch([xg.Config.from_text(t) for t in texts])
+    assert a.lib.xf_batch_set_shape(a.h, 8, bpw) == 0
+    b = xg.Batch([xg.Config.from_text(t) for t in texts])
+    assert b.lib.xf_batch_set_persistent(b.h, 1, bpw) == 0
+    oa, ob = a.run(max_iters=60), b.run(max_iters=60)
+    assert list(oa["iterations"]) == list(ob["iterations"]) and list(oa["accepted"]) == list(ob["accepted"])
+    for i in range(len(texts)):
+        assert np.array_equal(a.get_state(i), b.get_state(i))
+
+
+def test_batch_persistent_rejects_mixed():
+    b = xg.Batch([xg.Config.from_text(t) for t in _small_sweep("mixed", n=2)])
+    assert b.lib.xf_batch_set_persistent(b.h, 1, 1) == xg._abi.XF_EUNSUPPORTED

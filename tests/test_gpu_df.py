@@ -174,3 +174,27 @@ def test_maa_workload_shape_window_vs_fp64():
     assert (oa["iterations"], oa["accepted"]) == (ob["iterations"], ob["accepted"])
     assert abs(ob["last_max_err"] - oa["last_max_err"]) <= 1e-5 * oa["last_max_err"]
     assert np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0)))) <= 1e-11
+
+
+# ------------------------------------------------------------------ normal hierarchy
+
+@pytest.mark.parametrize("base,over", [
+    ("config0_ma.txt", dict(Abins=64, Ebins=64, R0=20, dr="1e-5")),
+    ("config1_ma.txt", dict(Abins=128, Ebins=128, R0=50, dr="1.5e-4")),
+    ("config3_maa.txt", dict(Abins=16, Pbins=8, Ebins=32, R0=15, dr="1e-6")),
+])
+def test_normal_hierarchy_vs_fp64(base, over):
+    """dm2 = +3e-3 eV^2 (src/Parser.cpp:99-100: the hierarchy is the sign of
+    dm2): free runs take FP64's decisions, and FP64's accepted steps replayed
+    in double-float stay within the FP64 parity bar."""
+    text = derive(base, dm2="3E-3", **over)
+    a, b = _pair(text, 3, 1e-6)
+    oa = a.evolutionLoop(max_iters=300, device_control=True, log_cap=300)
+    ob = b.evolutionLoop(max_iters=300, device_control=True)
+    assert (oa["iterations"], oa["accepted"]) == (ob["iterations"], ob["accepted"])
+    assert np.max(np.abs(pee(a.get_state(0)) - pee(b.get_state(0)))) <= 1e-8
+    c = xg.Simulation(xg.Config.from_text(_df(text)))
+    c.set_state(noise_state(c.nbeams, c.ebins, 3, 1e-6))
+    rb, dr = replay_inputs(text, oa["log"][:oa["accepted"]])
+    c.replay(rb, dr)
+    assert pol_rel_err(c.get_state(0), a.get_state(0)) <= POL_TOL

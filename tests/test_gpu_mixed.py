@@ -152,3 +152,21 @@ def test_renormalised_sums_match_oracle(geom):
         port.probe(r, dr)
         ref = port.calc_hvv(0, pt).reshape(-1)
         assert np.max(np.abs(h - ref)) <= 1e-12 * np.max(np.abs(ref)), pt
+
+
+@pytest.mark.parametrize("base,over", [
+    ("config0_ma.txt", dict(Abins=64, Ebins=64, R0=20, dr="1e-5")),
+    ("config1_ma.txt", dict(Abins=128, Ebins=128, R0=50, dr="1.5e-4")),
+    ("config3_maa.txt", dict(Abins=16, Pbins=8, Ebins=32, R0=15, dr="1e-6")),
+])
+def test_normal_hierarchy_vs_fp64(base, over):
+    """dm2 = +3e-3 eV^2 (src/Parser.cpp:99-100: the hierarchy is the sign of
+    dm2): the free run follows FP64's steps to within two, and FP64's accepted
+    steps replayed in mixed precision end within 1e-5 in P_ee(E)."""
+    text = derive(base, dm2="3E-3", **over)
+    a, b = _pair(text, 3, 1e-6)
+    oa = a.evolutionLoop(max_iters=300, device_control=True, log_cap=300)
+    ob = b.evolutionLoop(max_iters=300, device_control=True)
+    assert abs(oa["accepted"] - ob["accepted"]) <= 2
+    d = _replayed_dpee(text, a, oa, 3, 1e-6)
+    assert d <= 1e-5, d

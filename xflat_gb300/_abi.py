@@ -113,6 +113,7 @@ PROTOTYPES = {
     "xf_batch_tile_shape": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_double_p]),
     "xf_batch_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_double_p]),
     "xf_batch_set_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "xf_batch_set_persistent": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }
 
 _lib = None

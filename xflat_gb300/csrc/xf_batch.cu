@@ -30,6 +30,7 @@
 #include "xf_df.cuh"
 #include "xf_fp64.cuh"
 #include "xf_mixed.cuh"
+#include "xf_persist.cuh"
 #include "xflat_gpu.h"
 
 using xf::Ctl;
@@ -108,6 +109,51 @@ __global__ void __launch_bounds__(256, batch_min_blocks<PREC, PH>()) k_batch_pha
     }
 }
 
+template <int PREC, int PH>
+__device__ __forceinline__ void tile_phase(const Dev* __restrict__ devs, const Tile& t)
+{
+    const Dev& d = devs[t.inst];
+    const RedTarget rt = tile_target(d, t, PH);
+    const int nw = blockDim.x >> 5;
+    if (PREC == XF_PREC_FP64) {
+        if (PH == xf::PH_A) xf::fp64::phaseA_body<0>(d, t.first, nw, rt, t.end);
+        else if (PH == xf::PH_B) xf::fp64::phaseB_body<0>(d, t.first, nw, rt, t.end);
+        else xf::fp64::phaseC_body<0>(d, t.first, nw, rt, t.end);
+    } else {
+        if (PH == xf::PH_A) xf::dfp::phaseA_body<0>(d, t.first, nw, rt, t.end);
+        else if (PH == xf::PH_B) xf::dfp::phaseB_body<0>(d, t.first, nw, rt, t.end);
+        else xf::dfp::phaseC_body<0>(d, t.first, nw, rt, t.end);
+    }
+}
+
+// Persistent form of `iters` batch iterations (FP64 and double-float): one
+// cooperative launch whose blocks stride over the angle list and then over
+// the tile list of each phase, the stages separated by bounded grid barriers
+// (xf_persist.cuh) on the batch's own counter and timeout flag.
+template <int PREC>
+__global__ void __launch_bounds__(256, 2) k_batch_persist(const Dev* __restrict__ devs, const Tile* __restrict__ tiles,
+                                                          int ntiles, const int2* __restrict__ angles, int nang,
+                                                          int iters, unsigned int* bar, int* timeout, unsigned extra,
+                                                          unsigned long long limit_ns)
+{
+    unsigned gen = 0;
+    const auto at = [&](int i, int& ang) {
+        const int2 a = angles[i];
+        ang = a.y;
+        return &devs[a.x];
+    };
+    for (int i = 0; i < iters; ++i) {
+        geometry_pass(nang, at);
+        if (!grid_barrier(bar, timeout, gen, extra, limit_ns)) return;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) tile_phase<PREC, xf::PH_A>(devs, tiles[t]);
+        if (!grid_barrier(bar, timeout, gen, extra, limit_ns)) return;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) tile_phase<PREC, xf::PH_B>(devs, tiles[t]);
+        if (!grid_barrier(bar, timeout, gen, extra, limit_ns)) return;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) tile_phase<PREC, xf::PH_C>(devs, tiles[t]);
+        if (!grid_barrier(bar, timeout, gen, extra, limit_ns)) return;
+    }
+}
+
 // Mixed precision: flagged renormalisation with exact energy sums (warp tiles)
 // and the refreshed moments of psi0 (thread tiles of 256 beams).
 __global__ void __launch_bounds__(256) k_batch_renorm(const Dev* __restrict__ devs, const Tile* __restrict__ tiles)
@@ -150,6 +196,9 @@ double now_s()
 struct xf_batch {
     std::vector<xf_handle*> h;
     int prec = XF_PREC_FP64;
+    int persistent = 0;             // iterations as one cooperative launch (FP64, df; 8-warp tiles)
+    unsigned int* d_bar = nullptr;  // persistent form: [0] barrier arrivals, [1] timeout flag
+    int pblocks = 0;                // persistent form: resident blocks
     int warps = 8;                  // warps per block
     int bpw = 1;                    // beams per warp (a tile holds warps x bpw beams)
     cudaStream_t st = nullptr;
@@ -276,6 +325,42 @@ void launch_iteration(xf_batch* b)
     }
 }
 
+// One cooperative launch of k iterations and the status copy (the persistent
+// counterpart of a k-iteration graph launch).
+int launch_persistent(xf_batch* b, int k)
+{
+    const int n = (int)b->h.size();
+    void* fn = b->prec == XF_PREC_DF ? reinterpret_cast<void*>(k_batch_persist<XF_PREC_DF>)
+                                     : reinterpret_cast<void*>(k_batch_persist<XF_PREC_FP64>);
+    if (!b->pblocks) {
+        int dev = 0, sms = 152, occ = 0;
+        XB_CUDA(b, cudaGetDevice(&dev));
+        XB_CUDA(b, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        XB_CUDA(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 256, 0));
+        if (occ < 1) return b->fail(XF_ECUDA, "persistent batch kernel cannot be resident");
+        b->pblocks = std::min(occ * sms, std::max(b->nwt, (b->nang + 63) / 64));
+    }
+    if (!b->d_bar) XB_CUDA(b, cudaMalloc(&b->d_bar, 2 * sizeof(unsigned int)));
+    XB_CUDA(b, cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned int), b->st));
+    const Dev* dv = b->d_devs;
+    const Tile* wt = b->d_wtiles;
+    const int2* an = b->d_angles;
+    int nt = b->nwt, na = b->nang, it = k;
+    unsigned int* bar = b->d_bar;
+    int* tmo = reinterpret_cast<int*>(b->d_bar + 1);
+    unsigned extra = 0;
+    unsigned long long limit = 2000000000ull;
+    void* args[] = {&dv, &wt, &nt, &an, &na, &it, &bar, &tmo, &extra, &limit};
+    XB_CUDA(b, cudaLaunchCooperativeKernel(fn, dim3(b->pblocks), dim3(256), args, 0, b->st));
+    k_batch_status<<<(n + 63) / 64, 64, 0, b->st>>>(b->d_devs, n, b->d_status);
+    XB_CUDA(b, cudaMemcpyAsync(b->h_status, b->d_status, n * sizeof(Status), cudaMemcpyDeviceToHost, b->st));
+    unsigned int flag[2] = {0, 0};
+    XB_CUDA(b, cudaMemcpyAsync(flag, b->d_bar, sizeof(flag), cudaMemcpyDeviceToHost, b->st));
+    XB_CUDA(b, cudaStreamSynchronize(b->st));
+    if (flag[1]) return b->fail(XF_ETIMEOUT, "persistent batch: a grid-barrier wait ran out");
+    return XF_OK;
+}
+
 int get_graph(xf_batch* b, int k, cudaGraphExec_t* out)
 {
     for (auto& g : b->graphs)
@@ -319,14 +404,19 @@ int run(xf_batch* b, long max_iters, bool resume, double* device_ms)
         if (rc) return b->fail(rc, "instance " + std::to_string(i) + ": " + h->err);
     }
     const int k = 8;
-    cudaGraphExec_t ex;
+    cudaGraphExec_t ex = nullptr;
     int rc;
-    if ((rc = get_graph(b, k, &ex))) return rc;
+    const bool pers = b->persistent && b->prec != XF_PREC_MIXED;
+    if (!pers && (rc = get_graph(b, k, &ex))) return rc;
     XB_CUDA(b, cudaEventRecord(b->e0, b->st));
     long done_iters = 0;
     while (true) {
-        XB_CUDA(b, cudaGraphLaunch(ex, b->st));
-        XB_CUDA(b, cudaStreamSynchronize(b->st));
+        if (pers) {
+            if ((rc = launch_persistent(b, k))) return rc;
+        } else {
+            XB_CUDA(b, cudaGraphLaunch(ex, b->st));
+            XB_CUDA(b, cudaStreamSynchronize(b->st));
+        }
         done_iters += k;
         bool all = true;
         for (int i = 0; i < n; ++i) all = all && b->h_status[i].done;
@@ -424,6 +514,7 @@ int xf_batch_destroy(xf_batch* b)
     if (b->d_part) cudaFree(b->d_part);
     if (b->d_status) cudaFree(b->d_status);
     if (b->h_status) cudaFreeHost(b->h_status);
+    if (b->d_bar) cudaFree(b->d_bar);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
     if (b->st) cudaStreamDestroy(b->st);
@@ -487,7 +578,17 @@ int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms)
 int xf_batch_set_shape(xf_batch* b, int warps, int beams_per_warp)
 {
     if (!b || warps < 1 || warps > 8 || beams_per_warp < 1 || beams_per_warp > 64) return XF_EINVAL;
+    if (b->persistent && warps != 8) return b->fail(XF_EINVAL, "the persistent batch runs 8-warp tiles");
     return build_lists(b, warps, beams_per_warp);
+}
+
+int xf_batch_set_persistent(xf_batch* b, int on, int beams_per_warp)
+{
+    if (!b || beams_per_warp < 1 || beams_per_warp > 64) return XF_EINVAL;
+    if (on && b->prec == XF_PREC_MIXED) return b->fail(XF_EUNSUPPORTED, "the persistent batch serves FP64 and df");
+    b->persistent = on ? 1 : 0;
+    b->pblocks = 0;
+    return on ? build_lists(b, 8, beams_per_warp) : XF_OK;
 }
 
 int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* ncand, int* cand_warps, int* cand_bpw,

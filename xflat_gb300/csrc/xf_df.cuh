@@ -385,8 +385,8 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
             DK k1;
             if (GEOM == 0) {
                 // MA: dl1 = 2 dl0, so the halved U(dl1) has C1/2 - 1/2 = C0^2 - 1 =
-                // cm0 (2 + cm0) and S1/2 = C0 S0 = S0 + cm0 S0
-                k1.cm = lmul(k0.cm, ladd_big(DF{2.f, 0.f}, k0.cm));
+                // 2 cm0 + cm0^2 and S1/2 = C0 S0 = S0 + cm0 S0
+                k1.cm = ladd(dscale(2.f, k0.cm), lsq(k0.cm));
                 k1.S = ladd_big(k0.S, lmul(k0.cm, k0.S));
             } else {
                 k1 = dcoeffs<1>(a00, a01, g01i2, bm1);

@@ -6,85 +6,22 @@
 // launch gaps, prologues and reduction tails; here every block stays resident
 // and goes on to the next phase as soon as the barrier opens.
 //
-// Every barrier wait is bounded: a block whose wait runs past the limit
-// (default 2 s, set by the "barrier_timeout_ms" option) raises the control
-// block's timeout flag and returns, and the blocks still waiting see the flag
-// and return too, so the launch ends and the host reports XF_ETIMEOUT with
-// the context intact.  A cooperative launch guarantees that every block is
-// resident, so the waits end unless a block has stopped; the
-// "debug_barrier_extra" option makes each barrier wait for arrivals that never
-// come, which is how the tests exercise the limit.
+// Every barrier wait is bounded (grid_barrier, xf_persist.cuh): the limit is
+// 2 s by default, set by the "barrier_timeout_ms" option; the flag and the
+// arrival counter live in the control block.  The "debug_barrier_extra"
+// option makes each barrier wait for arrivals that never come, which is how
+// the tests exercise the limit.
 #include <cuda_runtime.h>
 
 #include "xf_df.cuh"
 #include "xf_fp64.cuh"
 #include "xf_mixed.h"
+#include "xf_persist.cuh"
 
 namespace xf {
 namespace {
 
 using namespace detail;
-
-__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p)
-{
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ int ld_relaxed(const int* p)
-{
-    int v;
-    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Grid-wide barrier on the control block's arrival counter (reset to zero
-// before each launch).  Returns false when this block's wait ran out or
-// another block's did.
-__device__ bool grid_barrier(Ctl* ctl, unsigned& gen, unsigned extra, unsigned long long limit_ns)
-{
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        ++gen;
-        const unsigned target = gen * (gridDim.x + extra);
-        __threadfence();  // this block's writes before its arrival
-        atomicAdd(&ctl->bar, 1u);
-        const unsigned long long t0 = globaltimer_ns();
-        int ok = 1;
-        for (unsigned polls = 1;; ++polls) {
-            if (ld_acquire(&ctl->bar) >= target) break;
-            if (ld_relaxed(&ctl->bar_timeout)) {
-                ok = 0;
-                break;
-            }
-            if ((polls & 31) == 0 && globaltimer_ns() - t0 > limit_ns) {
-                atomicExch(&ctl->bar_timeout, 1);
-                ok = 0;
-                break;
-            }
-            __nanosleep(64);
-        }
-        __threadfence();  // the other blocks' writes before this block's next loads
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-// The geometry of the three stage points, 64 angles x 3 points per block pass.
-__device__ void geometry_all(const Dev& d)
-{
-    __shared__ double s_c[3 * 64];
-    const int slot = threadIdx.x % 64, pt = threadIdx.x / 64;
-    const int groups = (d.A + 63) / 64;
-    for (int g = blockIdx.x; g < groups; g += gridDim.x) {
-        const int ang = g * 64 + slot;
-        geometry_point(d, (pt < 3 && ang < d.A) ? ang : -1, pt < 3 ? pt : 0, slot, 64, s_c);
-        __syncthreads();  // s_c is rewritten by the next pass
-    }
-}
 
 template <int PREC, int GEOM>
 __global__ void __launch_bounds__(256, 2) k_persist(Dev d, int iters, unsigned extra, unsigned long long limit_ns)
@@ -92,18 +29,24 @@ __global__ void __launch_bounds__(256, 2) k_persist(Dev d, int iters, unsigned e
     Ctl* ctl = d.ctl;
     unsigned gen = 0;
     const int w0 = blockIdx.x * (blockDim.x >> 5), ws = gridDim.x * (blockDim.x >> 5);
+    const auto at = [&](int i, int& ang) {
+        ang = i;
+        return &d;
+    };
+    unsigned* bar = &ctl->bar;
+    int* tmo = &ctl->bar_timeout;
     for (int i = 0; i < iters; ++i) {
-        geometry_all(d);
-        if (!grid_barrier(ctl, gen, extra, limit_ns)) return;
+        geometry_pass(d.A, at);
+        if (!grid_barrier(bar, tmo, gen, extra, limit_ns)) return;
         if (PREC == XF_PREC_DF) dfp::phaseA_body<GEOM>(d, w0, ws, grid_target(d, PH_A));
         else fp64::phaseA_body<GEOM>(d, w0, ws, grid_target(d, PH_A));
-        if (!grid_barrier(ctl, gen, extra, limit_ns)) return;
+        if (!grid_barrier(bar, tmo, gen, extra, limit_ns)) return;
         if (PREC == XF_PREC_DF) dfp::phaseB_body<GEOM>(d, w0, ws, grid_target(d, PH_B));
         else fp64::phaseB_body<GEOM>(d, w0, ws, grid_target(d, PH_B));
-        if (!grid_barrier(ctl, gen, extra, limit_ns)) return;
+        if (!grid_barrier(bar, tmo, gen, extra, limit_ns)) return;
         if (PREC == XF_PREC_DF) dfp::phaseC_body<GEOM>(d, w0, ws, grid_target(d, PH_C));
         else fp64::phaseC_body<GEOM>(d, w0, ws, grid_target(d, PH_C));
-        if (!grid_barrier(ctl, gen, extra, limit_ns)) return;
+        if (!grid_barrier(bar, tmo, gen, extra, limit_ns)) return;
         if (ld_relaxed(&ctl->done)) return;
     }
 }
