@@ -268,15 +268,20 @@ def accuracy_vs(xg, text, prec, psi_start, r0, log, psi_ref, surv_ref):
 
 def timed_run(xg, text, psi_start, r0, dr0, steps, warmup, log=False, options=None):
     """Device-controlled run of `steps` iterations from (r0, dr0) and the
-    start state, after `warmup` iterations from the same start."""
+    start state, after `warmup` iterations from the same start, in the
+    library's default launch form (a persistent cooperative launch where that
+    is faster); then the same steps again with per-phase CUDA events (the
+    graph-launched form), for the phase times."""
     sim = xg.Simulation(xg.Config.from_text(text))
     for k, v in (options or {}).items():
         sim.lib.xf_set_option(sim.h, k.encode(), float(v))
     sim.set_state(psi_start)
     sim.evolutionLoop(max_iters=max(3, warmup), device_control=True, iters_per_launch=16, r0=r0, dr0=dr0)
     sim.set_state(psi_start)
+    sim.evolutionLoop(max_iters=steps, device_control=True, iters_per_launch=16, r0=r0, dr0=dr0, time_phases=True)
+    sim.set_state(psi_start)
     out = sim.evolutionLoop(max_iters=steps, device_control=True, iters_per_launch=16, r0=r0, dr0=dr0,
-                            time_phases=True, log_cap=steps if log else 0)
+                            log_cap=steps if log else 0)
     return sim, out
 
 
@@ -431,6 +436,7 @@ def ours(args, rank, world, dist):
     if dist:
         dist.barrier()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        # FP64 at this size runs graph-launched phases; their CUDA events give the phase times
         st = sim.evolutionLoop(max_iters=args.steps, device_control=True, iters_per_launch=min(16, args.steps),
                                r0=R_START, dr0=DR_START, time_phases=True, log_cap=args.steps)
     if dist:

@@ -148,7 +148,14 @@ int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins)
  * sets how many energy-loop iterations ahead the mixed and double-float phase
  * kernels prefetch the state rows into L1 (default 1, 0 = none);
  * "df_b_occupancy" (2 or 3, default 2) picks the double-float phase-B kernel
- * built for that many resident blocks per SM; "debug_psi3" = 1 makes the last
+ * built for that many resident blocks per SM; "persistent" (1, 0, or -1 for
+ * the default choice by size and precision) runs a device-controlled xf_run
+ * of FP64 or double-float as one cooperative launch per iters_per_launch
+ * iterations, the stages separated by grid barriers whose waits are bounded
+ * by "barrier_timeout_ms" (default 2000; XF_ETIMEOUT when one runs out;
+ * "debug_barrier_extra" > 0 makes every wait run out, for tests), not when
+ * time_phases is set; "fp64_fused" = 1 folds the FP64 averages of phases B
+ * and C into their FMA chains (other rounding); "debug_psi3" = 1 makes the last
  * phase also store U(h4, dl2) psi3 into psi3, as the reference's in-place
  * stage S10 does (src/Nmr.cpp:191). */
 int xf_set_option(xf_handle* h, const char* name, double value);

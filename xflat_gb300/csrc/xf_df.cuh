@@ -34,8 +34,8 @@
 // term, energy weights and path lengths come from pair tables.  Moments are
 // accumulated in pairs, scaled by kappa (add_moment_df), and reduced across
 // blocks in FP64.  psi0 and the candidate share the mixed path's
-// compensated-pair buffers; psi1 and psi3 are pairs stored in the FP64
-// path's buffers ([nbeams][4][epad] hi, then lo).
+// compensated-pair buffers; psi1 and psi3 are pairs stored bin by bin in the
+// FP64 path's buffers (bin_ptr).
 #pragma once
 #include "xf_mixed.cuh"
 
@@ -284,6 +284,35 @@ __device__ __forceinline__ DF4 dapply(float q, const DK& k, const DF4& x, const 
     return y;
 }
 
+// a0 b0 + a1 b1 + a2 b2 + a3 b3.
+__device__ __forceinline__ DF ldot4(const DF& a0, const DF& b0, const DF& a1, const DF& b1, const DF& a2, const DF& b2,
+                                   const DF& a3, const DF& b3)
+{
+    const DF p = two_prod(a0.h, b0.h), q = two_prod(a1.h, b1.h), r = two_prod(a2.h, b2.h), u = two_prod(a3.h, b3.h);
+    const DF s1 = two_sum(p.h, q.h);
+    const DF s2 = two_sum(r.h, u.h);
+    const DF s = two_sum(s1.h, s2.h);
+    const float lo = (fmaf(a0.h, b0.l, fmaf(a0.l, b0.h, p.l)) + fmaf(a1.h, b1.l, fmaf(a1.l, b1.h, q.l))) +
+                     (fmaf(a2.h, b2.l, fmaf(a2.l, b2.h, r.l)) + fmaf(a3.h, b3.l, fmaf(a3.l, b3.h, u.l)));
+    return DF{s.h, ((s1.l + s2.l) + s.l) + lo};
+}
+
+// y = U x = (q + cm) x - i S sigma(h) x as one four-term sum per component,
+// with S folded into the Hamiltonian (z = S h, three products per bin): the
+// form for a propagator that shares nothing with another.
+__device__ __forceinline__ DF4 dapply_z(float q, const DK& k, const DF& h00, const DF& h01r, const DF& h01i,
+                                        const DF4& x)
+{
+    const DF c = ladd_big(DF{q, 0.f}, k.cm);
+    const DF z0 = lmul(k.S, h00), zr = lmul(k.S, h01r), zi = lmul(k.S, h01i);
+    DF4 y;
+    y.ar = ldot4(c, x.ar, z0, x.ai, zi, x.br, zr, x.bi);
+    y.ai = ldot4(c, x.ai, neg(z0), x.ar, zi, x.bi, neg(zr), x.br);
+    y.br = ldot4(c, x.br, neg(zi), x.ar, zr, x.ai, neg(z0), x.bi);
+    y.bi = ldot4(c, x.bi, neg(zi), x.ai, neg(zr), x.ar, z0, x.br);
+    return y;
+}
+
 __device__ __forceinline__ DF4 dadd4(const DF4& a, const DF4& b)
 {
     DF4 c;
@@ -331,9 +360,39 @@ __device__ __forceinline__ void reduce_sums(DF (&v)[NV], int lane)
     mixed::df_reduce_scatter<NV>(v, lane);
 }
 
-// psi1 / psi3 pair buffers inside the FP64 path's double buffers.
-__device__ __forceinline__ float* pair_hi(double* buf) { return reinterpret_cast<float*>(buf); }
-__device__ __forceinline__ size_t pair_span(const Dev& d) { return (size_t)d.nbeams * 4 * d.epad; }
+// psi1 / psi3, which only this path reads, in the FP64 path's buffers laid
+// out bin by bin: [beam][ebin][8] floats, the four components' hi parts then
+// their lo parts, so a lane moves a bin with two 16-byte accesses and a warp
+// 1 KB of contiguous memory.
+__device__ __forceinline__ float* bin_ptr(double* buf, int epad, int b, int e)
+{
+    return reinterpret_cast<float*>(buf) + ((size_t)b * epad + e) * 8;
+}
+
+__device__ __forceinline__ DF4 load_bin(const float* __restrict__ p)
+{
+    const float4 h = *reinterpret_cast<const float4*>(p), l = *reinterpret_cast<const float4*>(p + 4);
+    DF4 x;
+    x.ar = DF{h.x, l.x};
+    x.ai = DF{h.y, l.y};
+    x.br = DF{h.z, l.z};
+    x.bi = DF{h.w, l.w};
+    return x;
+}
+
+// Stores a renormalised x.
+__device__ __forceinline__ void store_bin_raw(float* __restrict__ p, const DF4& x)
+{
+    *reinterpret_cast<float4*>(p) = make_float4(x.ar.h, x.ai.h, x.br.h, x.bi.h);
+    *reinterpret_cast<float4*>(p + 4) = make_float4(x.ar.l, x.ai.l, x.br.l, x.bi.l);
+}
+
+__device__ __forceinline__ void store_bin(float* __restrict__ p, const DF4& x) { store_bin_raw(p, norm4(x)); }
+
+__device__ __forceinline__ void prefetch_bin(const float* p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
 
 // ------------------------------------------------------------------ phase A
 
@@ -347,9 +406,6 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     __shared__ double s_out[32];
     const float* __restrict__ h0 = ctl->m0hi;
     const float* __restrict__ l0 = ctl->m0lo;
-    float* p1h = pair_hi(d.psi1);
-    float* p3h = pair_hi(d.psi3);
-    const size_t span = pair_span(d);
     const double hm = ctl->hm[0];
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
@@ -394,8 +450,8 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
             const DF4 w = dsig_w(a00, a01, g01i, x);
             const DF4 y1 = dapply(.5f, k1, x, w);
             const DF4 y3 = dapply(1.f, k0, x, w);
-            store_df(p1h + base, p1h + span + base, epad, e, y1);
-            store_df(p3h + base, p3h + span + base, epad, e, y3);
+            store_bin(bin_ptr(d.psi1, epad, b, e), y1);
+            store_bin(bin_ptr(d.psi3, epad, b, e), y3);
             const DF f = fv_df(d, bi.p, e);
             dacc_rho(y1, f, v[0], v[1], v[2]);
             dacc_rho(y3, f, v[3], v[4], v[5]);
@@ -437,8 +493,6 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     const float* __restrict__ l0 = ctl->m0lo;
     float* h4 = ctl->m4hi;
     float* l4 = ctl->m4lo;
-    float* p1h = pair_hi(d.psi1);
-    const size_t span = pair_span(d);
     const double hm_rdr = ctl->hm[2], hm_rdr2 = ctl->hm[1];
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
@@ -463,21 +517,20 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             if (pf && e + pf < epad) {
                 prefetch_rows(h0 + base, epad, e + pf);
                 prefetch_rows(l0 + base, epad, e + pf);
-                prefetch_rows(p1h + base, epad, e + pf);
-                prefetch_rows(p1h + span + base, epad, e + pf);
+                prefetch_bin(bin_ptr(d.psi1, epad, b, e + pf));
             }
             const DF hv0 = hv_df(d, 0, e), hv1 = hv_df(d, 1, e);
             const DF4 x = load_df(h0 + base, l0 + base, epad, e);
             // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
             const DF a00 = ladd(hv0, g100), a01 = ladd(hv1, g101r);
             const DK ka = dcoeffs<1>(a00, a01, ga2, bl);
-            const DF4 ya = dapply(.5f, ka, x, dsig_w(a00, a01, g101i, x));
-            const DF4 p1 = load_df(p1h + base, p1h + span + base, epad, e);
-            store_df(p1h + base, p1h + span + base, epad, e, dadd4(ya, p1));
+            const DF4 ya = dapply_z(.5f, ka, a00, a01, g101i, x);
+            float* p1p = bin_ptr(d.psi1, epad, b, e);
+            store_bin(p1p, dadd4(ya, load_bin(p1p)));
             // S8, stored halved for the average of S10/S11
             const DF b00 = ladd(hv0, g300), b01 = ladd(hv1, g301r);
             const DK kb = dcoeffs<1>(b00, b01, gb2, bl);
-            const DF4 y4 = dapply(.5f, kb, x, dsig_w(b00, b01, g301i, x));
+            const DF4 y4 = dapply_z(.5f, kb, b00, b01, g301i, x);
             store_df(h4 + base, l4 + base, epad, e, y4);
             dacc_rho(y4, fv_df(d, bi.p, e), v[0], v[1], v[2]);
         }
@@ -511,9 +564,6 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     float* l4 = ctl->m4lo;
     double* __restrict__ S4 = ctl->S4;
     float2* __restrict__ S4f = ctl->S4f;
-    const float* p1h = pair_hi(d.psi1);
-    const float* p3h = pair_hi(d.psi3);
-    const size_t span = pair_span(d);
     const double hm_rdr = ctl->hm[2];
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
@@ -536,24 +586,22 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         float err = 0.f;
         for (int e = lane; e < epad; e += 32) {
             if (pf && e + pf < epad) {
-                prefetch_rows(p3h + base, epad, e + pf);
-                prefetch_rows(p3h + span + base, epad, e + pf);
+                prefetch_bin(bin_ptr(d.psi3, epad, b, e + pf));
                 prefetch_rows(h4 + base, epad, e + pf);
                 prefetch_rows(l4 + base, epad, e + pf);
-                prefetch_rows(p1h + base, epad, e + pf);
-                prefetch_rows(p1h + span + base, epad, e + pf);
+                prefetch_bin(bin_ptr(d.psi1, epad, b, e + pf));
             }
             const DF a00 = ladd(hv_df(d, 0, e), g00), a01 = ladd(hv_df(d, 1, e), g01r);
-            const DF4 x3 = load_df(p3h + base, p3h + span + base, epad, e);
+            const DF4 x3 = load_bin(bin_ptr(d.psi3, epad, b, e));
             // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
             const DK k = dcoeffs<1>(a00, a01, g01i2, bm);
-            const DF4 y3 = dapply(.5f, k, x3, dsig_w(a00, a01, g01i, x3));
+            const DF4 y3 = dapply_z(.5f, k, a00, a01, g01i, x3);
             const DF4 c = norm4(dadd4(y3, load_df(h4 + base, l4 + base, epad, e)));
             store_raw(h4 + base, l4 + base, epad, e, c);
             // calcErrHvv against psi1: the hi parts of two states this close
             // differ exactly (Sterbenz), so the difference is exact to 2^-48
             // of the state, far below the error's own size
-            const DF4 r1 = load_df(p1h + base, p1h + span + base, epad, e);
+            const DF4 r1 = load_bin(bin_ptr(d.psi1, epad, b, e));
             const float e0 = (c.ar.h - r1.ar.h) + (c.ar.l - r1.ar.l), e1 = (c.ai.h - r1.ai.h) + (c.ai.l - r1.ai.l);
             const float e2 = (c.br.h - r1.br.h) + (c.br.l - r1.br.l), e3 = (c.bi.h - r1.bi.h) + (c.bi.l - r1.bi.l);
             const DF f = fv_df(d, bi.p, e);

@@ -586,8 +586,13 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
         log_cap_dev = o.log_cap;
     }
     const bool files = o.write_files && cfg.dump_mode != 0;
-    // the persistent loop serves FP64 and double-float; per-phase timing needs the graphs' events
-    const bool pers = persistent && (!mixed || dev.df) && !o.time_phases;
+    // the persistent loop serves FP64 and double-float; per-phase timing needs the graphs' events.
+    // Measured on GB300 (ms per iteration, graphs -> persistent): double-float 0.0512 -> 0.0500 at
+    // 65 K bins, 0.109 -> 0.102 at 524 K, 0.502 -> 0.483 at 4.19 M; FP64 0.0734 -> 0.0679 at 65 K,
+    // 0.280 -> 0.284 at 524 K, 1.70 -> 1.91 at 4.19 M.  The default takes it for double-float, and
+    // for FP64 when one wave of two 8-warp blocks per SM covers every beam.
+    const bool auto_pers = dev.df || (!mixed && nbeams <= 2 * 152 * 8);
+    const bool pers = (persistent > 0 || (persistent < 0 && auto_pers)) && (!mixed || dev.df) && !o.time_phases;
     if (files && (rc = io_dev_prepare(k))) return rc;
     if ((rc = start_device_run(r, dr, Ts, files))) return rc;
     // instantiate the graph sizes this run needs before the timed region starts
@@ -766,8 +771,11 @@ int xf_set_option(xf_handle* h, const char* name, double value)
         h->shape.blocks = b ? b : def.blocks;
         h->shape.blocks_ab = b ? b : def.blocks_ab;
         for (int p = 0; p < 3; ++p) h->shape.phase_blocks[p] = b ? b : def.phase_blocks[p];
+    } else if (n == "fp64_fused") {
+        h->shape.fp64_fused = value != 0.;
     } else if (n == "persistent") {
-        h->persistent = value != 0.;
+        if (value != -1. && value != 0. && value != 1.) return h->fail(XF_EINVAL, "persistent must be -1, 0 or 1");
+        h->persistent = (int)value;
     } else if (n == "barrier_timeout_ms") {
         if (!(value > 0.) || value > 60000.) return h->fail(XF_EINVAL, "barrier_timeout_ms must be in (0, 60000]");
         h->barrier_timeout_ms = value;
@@ -896,10 +904,12 @@ int xf_run(xf_handle* h, const xf_run_opts* opts, xf_step_cb cb, void* user, xf_
     h->launches = 0;
     h->h2d_bytes = h->d2h_bytes = 0;
     h->time_phases = o.time_phases;
-    for (int i = 0; i < 3; ++i) {
-        h->phase_ms[i] = 0.;
-        h->phase_n[i] = 0;
-    }
+    // xf_phase_times reports the last run that timed its phases
+    if (o.time_phases)
+        for (int i = 0; i < 3; ++i) {
+            h->phase_ms[i] = 0.;
+            h->phase_n[i] = 0;
+        }
     int rc;
     if (o.device_control) {
         if (cb) return h->fail(XF_EUNSUPPORTED, "per-step callbacks need the host-driven loop");

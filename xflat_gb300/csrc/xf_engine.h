@@ -60,7 +60,8 @@ struct xf_handle {
     int renorm_every = 16;        // mixed precision: accepted steps between renormalisations
     int accepts_since_renorm = 0;
     int time_phases = 0;
-    int persistent = 0;           // device control as one cooperative launch per k iterations (FP64, df)
+    int persistent = -1;          // device control as one cooperative launch per k iterations (FP64, df);
+                                  // -1: chosen by size and precision (persistent_default)
     double barrier_timeout_ms = 2000.;  // limit of each grid-barrier wait of the persistent loop
     int barrier_extra = 0;        // test hook: arrivals each barrier waits for beyond the grid (never come)
     double phase_ms[3] = {0., 0., 0.};

@@ -129,6 +129,18 @@ __device__ __forceinline__ Psi su2_w(double h00, double h01r, double h01i, const
     return w;
 }
 
+// C x + S w + a in one FMA chain per component (the averages of S4/S5 and
+// S10/S11 without a separate addition; other rounding than su2_apply_w + a).
+__device__ __forceinline__ Psi su2_apply_w_add(double C, double S, const Psi& x, const Psi& w, const Psi& a)
+{
+    Psi y;
+    y.ar = fma(C, x.ar, fma(S, w.ar, a.ar));
+    y.ai = fma(C, x.ai, fma(S, w.ai, a.ai));
+    y.br = fma(C, x.br, fma(S, w.br, a.br));
+    y.bi = fma(C, x.bi, fma(S, w.bi, a.bi));
+    return y;
+}
+
 __device__ __forceinline__ Psi su2_apply_w(double C, double S, const Psi& x, const Psi& w)
 {
     Psi y;
@@ -141,9 +153,12 @@ __device__ __forceinline__ Psi su2_apply_w(double C, double S, const Psi& x, con
 
 // Accumulates fv * rho(psi) (first row of the density matrix, src/NBeam.cpp:314-322);
 // component 0 is accumulated without the factor 1/2, applied once per beam.
+template <int FUSE = 0>
 __device__ __forceinline__ void acc_rho(const Psi& x, double fv, double& s0, double& s2, double& s3)
 {
-    const double d0 = (x.ar * x.ar + x.ai * x.ai) - (x.br * x.br + x.bi * x.bi);
+    // FUSE: the four squares in one FMA chain (one operation fewer, other rounding)
+    const double d0 = FUSE ? fma(x.ar, x.ar, fma(x.ai, x.ai, -fma(x.br, x.br, x.bi * x.bi)))
+                           : (x.ar * x.ar + x.ai * x.ai) - (x.br * x.br + x.bi * x.bi);
     const double d2 = x.ar * x.br + x.ai * x.bi;
     const double d3 = x.ai * x.br - x.ar * x.bi;
     s0 = fma(d0, fv, s0);
@@ -258,7 +273,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 
 // S4/S5 (psi4' = U(h1, dl1, hm(r+dr)) psi0 averaged into psi1) and S8
 // (psi4 = U(h3, dl1, hm(r+dr/2)) psi0) with the moments of psi4 at point 2 (S9).
-template <int GEOM>
+template <int GEOM, int FUSE = 0>
 __device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
@@ -296,20 +311,24 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const double a00 = hv0 + g1.h00b, a01 = hv1 + g1.h01rb;
             // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
             su2_coeffs<1>(a00, a01, pka, C, S);
-            const Psi ya = su2_apply_w(C, S, x, su2_w(a00, a01, g1.h01i, x));
             const Psi p1 = load_psi(io1, epad, e);
             Psi avg;
-            avg.ar = ya.ar + p1.ar;
-            avg.ai = ya.ai + p1.ai;
-            avg.br = ya.br + p1.br;
-            avg.bi = ya.bi + p1.bi;
+            if (FUSE) {
+                avg = su2_apply_w_add(C, S, x, su2_w(a00, a01, g1.h01i, x), p1);
+            } else {
+                const Psi ya = su2_apply_w(C, S, x, su2_w(a00, a01, g1.h01i, x));
+                avg.ar = ya.ar + p1.ar;
+                avg.ai = ya.ai + p1.ai;
+                avg.br = ya.br + p1.br;
+                avg.bi = ya.bi + p1.bi;
+            }
             store_psi(io1, epad, e, avg);
             const double b00 = hv0 + g3.h00b, b01 = hv1 + g3.h01rb;
             // S8, stored halved for the average of S10/S11
             su2_coeffs<1>(b00, b01, pkb, C, S);
             const Psi y4 = su2_apply_w(C, S, x, su2_w(b00, b01, g3.h01i, x));
             store_psi(o4, epad, e, y4);
-            acc_rho(y4, fvp[e], v[0], v[1], v[2]);
+            acc_rho<FUSE>(y4, fvp[e], v[0], v[1], v[2]);
         }
         // psi4 was accumulated halved: its sums are a quarter (exactly) of psi4's
         v[0] *= 2.;
@@ -334,7 +353,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
 // max over beams (src/Nmr.cpp:195-206), and the moments of the candidate.
 // Under device control the last block also runs the step controller of
 // src/Nmr.cpp:227-249.
-template <int GEOM>
+template <int GEOM, int FUSE = 0>
 __device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
@@ -371,27 +390,32 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             double C, S;
             // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
             su2_coeffs<1>(a00, a01, pk, C, S);
-            const Psi y3 = su2_apply_w(C, S, x3, su2_w(a00, a01, g.h01i, x3));
-            if (d.debug_psi3) {
-                Psi full;
-                full.ar = 2. * y3.ar;
-                full.ai = 2. * y3.ai;
-                full.br = 2. * y3.br;
-                full.bi = 2. * y3.bi;
-                store_psi(io3, epad, e, full);
-            }
+            const Psi w3 = su2_w(a00, a01, g.h01i, x3);
             const Psi x4 = load_psi(io4, epad, e);
             Psi c;
-            c.ar = y3.ar + x4.ar;
-            c.ai = y3.ai + x4.ai;
-            c.br = y3.br + x4.br;
-            c.bi = y3.bi + x4.bi;
+            if (FUSE && !d.debug_psi3) {
+                c = su2_apply_w_add(C, S, x3, w3, x4);
+            } else {
+                const Psi y3 = su2_apply_w(C, S, x3, w3);
+                if (d.debug_psi3) {
+                    Psi full;
+                    full.ar = 2. * y3.ar;
+                    full.ai = 2. * y3.ai;
+                    full.br = 2. * y3.br;
+                    full.bi = 2. * y3.bi;
+                    store_psi(io3, epad, e, full);
+                }
+                c.ar = y3.ar + x4.ar;
+                c.ai = y3.ai + x4.ai;
+                c.br = y3.br + x4.br;
+                c.bi = y3.bi + x4.bi;
+            }
             store_psi(io4, epad, e, c);
             const Psi r1 = load_psi(p1b, epad, e);
             const double f = fvp[e];
             const double e0 = c.ar - r1.ar, e1 = c.ai - r1.ai, e2 = c.br - r1.br, e3 = c.bi - r1.bi;
             v[0] = fma((e0 * e0 + e1 * e1) + (e2 * e2 + e3 * e3), f, v[0]);
-            acc_rho(c, f, v[1], v[2], v[3]);
+            acc_rho<FUSE>(c, f, v[1], v[2], v[3]);
         }
         v[1] *= .5;
         warp_reduce_scatter<4>(v, lane);

@@ -69,11 +69,12 @@ __global__ void __launch_bounds__(256) k_phaseA(Dev d)
     fp64::phaseA_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_A));
 }
 
-template <int GEOM>
+template <int GEOM, int FUSE>
 __global__ void __launch_bounds__(256) k_phaseB(Dev d)
 {
     pdl_enter();
-    fp64::phaseB_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_B));
+    fp64::phaseB_body<GEOM, FUSE>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5),
+                                  grid_target(d, PH_B));
 }
 
 // Phase C holds fewer values across the energy loop than A and B: capped at
@@ -81,11 +82,12 @@ __global__ void __launch_bounds__(256) k_phaseB(Dev d)
 // with little or no spilling, and the extra warps hide FP64 latency (measured
 // on GB300: 0.535 -> 0.498 ms at 4.19M MA bins, 1.094 -> 1.024 ms at 8.39M
 // MAA bins; the same caps slow phases A and B).
-template <int GEOM>
+template <int GEOM, int FUSE>
 __global__ void __launch_bounds__(256, GEOM == 0 ? 3 : 4) k_phaseC(Dev d)
 {
     pdl_enter();
-    fp64::phaseC_body<GEOM>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5), grid_target(d, PH_C));
+    fp64::phaseC_body<GEOM, FUSE>(d, blockIdx.x * (blockDim.x >> 5), gridDim.x * (blockDim.x >> 5),
+                                  grid_target(d, PH_C));
 }
 
 // ------------------------------------------------------------------ helpers
@@ -251,16 +253,22 @@ void launch_moments(const Dev& d, const double* S, int pt, double* Jout, cudaStr
     else launch_pdl(k_moments<1>, blocks, t, st, d, S, pt, Jout, conditional);
 }
 
+template <int GEOM, int FUSE>
+void launch_phase_t(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
+{
+    if (phase == PH_A) launch_pdl(k_phaseA<GEOM>, sh.blocks, sh.threads, st, d);
+    else if (phase == PH_B) launch_pdl(k_phaseB<GEOM, FUSE>, sh.blocks, sh.threads, st, d);
+    else launch_pdl(k_phaseC<GEOM, FUSE>, sh.blocks, sh.threads, st, d);
+}
+
 void launch_phase(int phase, const Dev& d, const Shape& sh, cudaStream_t st)
 {
     if (d.geom == 0) {
-        if (phase == PH_A) launch_pdl(k_phaseA<0>, sh.blocks, sh.threads, st, d);
-        else if (phase == PH_B) launch_pdl(k_phaseB<0>, sh.blocks, sh.threads, st, d);
-        else launch_pdl(k_phaseC<0>, sh.blocks, sh.threads, st, d);
+        if (sh.fp64_fused) launch_phase_t<0, 1>(phase, d, sh, st);
+        else launch_phase_t<0, 0>(phase, d, sh, st);
     } else {
-        if (phase == PH_A) launch_pdl(k_phaseA<1>, sh.blocks, sh.threads, st, d);
-        else if (phase == PH_B) launch_pdl(k_phaseB<1>, sh.blocks, sh.threads, st, d);
-        else launch_pdl(k_phaseC<1>, sh.blocks, sh.threads, st, d);
+        if (sh.fp64_fused) launch_phase_t<1, 1>(phase, d, sh, st);
+        else launch_phase_t<1, 0>(phase, d, sh, st);
     }
 }
 
