@@ -378,8 +378,9 @@ def batched_leg(xg, steps):
         t = b.tuning()
         out["batched_" + prec] = {"value": units / r["seconds"], "unit": UNIT, "seconds": r["seconds"],
                                   "tile": {"warps_per_block": t["warps"], "beams_per_warp": t["beams_per_warp"],
-                                           "candidates_ms": {"%dx%d" % (w, bp): round(ms, 3)
-                                                             for w, bp, ms in t["candidates"]}}}
+                                           "launch": "persistent" if t["persistent"] else "graphs",
+                                           "candidates_ms": {"%s %dx%d" % ("persistent" if p else "graphs", w, bp):
+                                                             round(ms, 3) for w, bp, p, ms in t["candidates"]}}}
         states[prec] = ([b.get_state(i)[0::4, :2] for i in range(len(b.dims))], list(r["accepted"]))
         b.close()
     units, ms = 0, 0.0
@@ -407,13 +408,16 @@ def batched_leg(xg, steps):
 
 def whole_run_record():
     """The opt-in whole-run test's measured result (tests/test_gpu_full_run.py),
-    committed as profiles/whole_run_config0.json: recorded, not measured by
-    this run."""
-    path = os.path.join(ROOT, "profiles", "whole_run_config0.json")
+    committed in profiles/whole_run_config0.md as a line `record: {json}`:
+    recorded, not measured by this run."""
+    path = os.path.join(ROOT, "profiles", "whole_run_config0.md")
     if not os.path.exists(path):
         return None
-    rec = json.load(open(path))
-    rec["source"] = "profiles/whole_run_config0.json (tests/test_gpu_full_run.py on a GB300; not measured by this run)"
+    m = re.search(r"^record: (\{.*\})\s*$", open(path).read(), re.M)
+    if not m:
+        return None
+    rec = json.loads(m.group(1))
+    rec["source"] = "profiles/whole_run_config0.md (tests/test_gpu_full_run.py on a GB300; not measured by this run)"
     return rec
 
 

@@ -282,11 +282,13 @@ int xf_batch_run(xf_batch* b, long max_iters, long* iters, long* accepted, doubl
  * (may be NULL). */
 int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms);
 /* The autotuner's full table: the chosen warps per block (block size 32 x
- * warps) and beams per warp (blocks per phase = beams / (warps x beams per
- * warp)), and for each of the *ncand (<= 16) candidates its shape and the
- * measured time (ms, 8 iterations of the whole batch).  Any output may be NULL. */
-int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* ncand, int* cand_warps, int* cand_bpw,
-                    double* cand_ms);
+ * warps), beams per warp (blocks per phase = beams / (warps x beams per
+ * warp)) and launch form (persistent 1: one cooperative launch per 8
+ * iterations, 0: graphs of per-stage launches), and for each of the *ncand
+ * (<= 16) candidates its shape, form and measured time (ms, 8 iterations of
+ * the whole batch).  Any output may be NULL. */
+int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* persistent, int* ncand, int* cand_warps,
+                    int* cand_bpw, int* cand_persistent, double* cand_ms);
 /* Replaces the tuned tile shape: warps per block in [1, 8], beams per warp in
  * [1, 64]. */
 int xf_batch_set_shape(xf_batch* b, int warps, int beams_per_warp);
@@ -294,7 +296,7 @@ int xf_batch_set_shape(xf_batch* b, int warps, int beams_per_warp);
  * iterations (FP64 and df), the stages separated by grid barriers whose waits
  * are bounded (XF_ETIMEOUT when one runs out), over 8-warp tiles of
  * beams_per_warp beams per warp; on = 0: CUDA graphs of the per-stage
- * launches (the default). */
+ * launches.  Overrides the autotuner's choice. */
 int xf_batch_set_persistent(xf_batch* b, int on, int beams_per_warp);
 
 #ifdef __cplusplus

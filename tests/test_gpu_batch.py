@@ -40,8 +40,9 @@ def test_batch_uneven_budgets_and_radii():
     w, ms = b.tile_shape()
     assert w in (2, 4, 8) and np.all(ms > 0)
     t = b.tuning()
-    assert len(t["candidates"]) == 9 and all(c[2] > 0 for c in t["candidates"])
-    assert (t["warps"], t["beams_per_warp"]) == min(t["candidates"], key=lambda c: c[2])[:2]
+    # 9 graph-launched shapes and 3 persistent ones (FP64)
+    assert len(t["candidates"]) == 12 and all(c[3] > 0 for c in t["candidates"])
+    assert (t["warps"], t["beams_per_warp"], t["persistent"]) == min(t["candidates"], key=lambda c: c[3])[:3]
 
 
 @pytest.mark.parametrize("warps,bpw", [(2, 4), (8, 2)])
@@ -54,6 +55,7 @@ def test_batch_tile_shapes_agree(warps, bpw):
     ref = b.run(max_iters=40)
     ref_states = [b.get_state(i) for i in range(len(texts))]
     c = xg.Batch([xg.Config.from_text(t) for t in texts])
+    assert c.lib.xf_batch_set_persistent(c.h, 0, 1) == 0
     assert c.lib.xf_batch_set_shape(c.h, warps, bpw) == 0
     out = c.run(max_iters=40)
     assert list(out["accepted"]) == list(ref["accepted"])
@@ -130,6 +132,7 @@ def test_batch_persistent_equals_graphs(prec, bpw):
     tile shape: the same decisions and states bit for bit."""
     texts = _small_sweep(prec)
     a = xg.Batch([xg.Config.from_text(t) for t in texts])
+    assert a.lib.xf_batch_set_persistent(a.h, 0, 1) == 0
     assert a.lib.xf_batch_set_shape(a.h, 8, bpw) == 0
     b = xg.Batch([xg.Config.from_text(t) for t in texts])
     assert b.lib.xf_batch_set_persistent(b.h, 1, bpw) == 0

@@ -298,14 +298,14 @@ class Batch:
 
     def tuning(self):
         """The autotuner's choice and table: {'warps', 'beams_per_warp',
-        'candidates': [(warps, beams_per_warp, ms), ...]}."""
-        w, bpw, nc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        cw, cb = (ctypes.c_int * 16)(), (ctypes.c_int * 16)()
+        'persistent', 'candidates': [(warps, beams_per_warp, persistent, ms), ...]}."""
+        w, bpw, pers, nc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        cw, cb, cp = (ctypes.c_int * 16)(), (ctypes.c_int * 16)(), (ctypes.c_int * 16)()
         ms = np.zeros(16)
-        self._c(self.lib.xf_batch_tuning(self.h, ctypes.byref(w), ctypes.byref(bpw), ctypes.byref(nc), cw, cb, _dp(ms)),
-                "xf_batch_tuning")
-        return dict(warps=w.value, beams_per_warp=bpw.value,
-                    candidates=[(cw[i], cb[i], float(ms[i])) for i in range(nc.value)])
+        self._c(self.lib.xf_batch_tuning(self.h, ctypes.byref(w), ctypes.byref(bpw), ctypes.byref(pers),
+                                         ctypes.byref(nc), cw, cb, cp, _dp(ms)), "xf_batch_tuning")
+        return dict(warps=w.value, beams_per_warp=bpw.value, persistent=pers.value,
+                    candidates=[(cw[i], cb[i], cp[i], float(ms[i])) for i in range(nc.value)])
 
     def run(self, max_iters=-1):
         n = len(self.cfgs)

@@ -111,7 +111,8 @@ PROTOTYPES = {
     "xf_batch_get_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p]),
     "xf_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_long, c_long_p, c_long_p, c_double_p, c_double_p]),
     "xf_batch_tile_shape": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_double_p]),
-    "xf_batch_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_double_p]),
+    "xf_batch_tuning": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
+                                       c_double_p]),
     "xf_batch_set_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "xf_batch_set_persistent": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }

@@ -218,7 +218,7 @@ struct xf_batch {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     static constexpr int kMaxCand = 16;
     int ncand = 0;
-    int cand_warps[kMaxCand] = {}, cand_bpw[kMaxCand] = {};
+    int cand_warps[kMaxCand] = {}, cand_bpw[kMaxCand] = {}, cand_pers[kMaxCand] = {};
     double cand_ms[kMaxCand] = {};
     std::string err;
 
@@ -463,30 +463,41 @@ int xf_batch_create(const xf_config* cfgs, int n, xf_batch** out)
     if (rc == XF_OK && (cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess)) rc = XF_ECUDA;
     if (rc == XF_OK && cudaMalloc(&b->d_status, n * sizeof(Status)) != cudaSuccess) rc = XF_ENOMEM;
     if (rc == XF_OK && cudaMallocHost(&b->h_status, n * sizeof(Status)) != cudaSuccess) rc = XF_ENOMEM;
-    // autotune the tile shape on the batch itself: a few iterations per
-    // candidate (warps per block x beams per warp) from the initial states,
-    // which are restored afterwards
+    // autotune the launch form on the batch itself: a few iterations per
+    // candidate from the initial states, which are restored afterwards.  The
+    // candidates are the graph-launched stages with warps per block x beams
+    // per warp in {2, 4, 8} x {1, 2, 4}, and (FP64, df) the persistent form
+    // with 8-warp tiles of 1, 2 or 4 beams per warp.
     if (rc == XF_OK) {
         const int cw[3] = {2, 4, 8}, cb[3] = {1, 2, 4};
         double best = 1e300;
-        int best_w = 8, best_b = 1;
+        int best_w = 8, best_b = 1, best_p = 0;
         b->ncand = 0;
-        for (int i = 0; i < 3 && rc == XF_OK; ++i)
-            for (int j = 0; j < 3 && rc == XF_OK; ++j) {
-                rc = build_lists(b, cw[i], cb[j]);
-                double ms = 0.;
-                if (rc == XF_OK) rc = run(b, 2, false, nullptr);  // first launch instantiates the graph
-                if (rc == XF_OK) rc = run(b, 8, false, &ms);
-                const int c = b->ncand++;
-                b->cand_warps[c] = cw[i];
-                b->cand_bpw[c] = cb[j];
-                b->cand_ms[c] = ms;
-                if (rc == XF_OK && ms < best) {
-                    best = ms;
-                    best_w = cw[i];
-                    best_b = cb[j];
+        const int nforms = b->prec == XF_PREC_MIXED ? 1 : 2;
+        for (int f = 0; f < nforms && rc == XF_OK; ++f)
+            for (int i = 0; i < 3 && rc == XF_OK; ++i)
+                for (int j = 0; j < 3 && rc == XF_OK; ++j) {
+                    if (f == 1 && cw[i] != 8) continue;
+                    b->persistent = f;
+                    b->pblocks = 0;
+                    rc = build_lists(b, cw[i], cb[j]);
+                    double ms = 0.;
+                    if (rc == XF_OK) rc = run(b, 2, false, nullptr);  // the first launch instantiates the graph
+                    if (rc == XF_OK) rc = run(b, 8, false, &ms);
+                    const int c = b->ncand++;
+                    b->cand_warps[c] = cw[i];
+                    b->cand_bpw[c] = cb[j];
+                    b->cand_pers[c] = f;
+                    b->cand_ms[c] = ms;
+                    if (rc == XF_OK && ms < best) {
+                        best = ms;
+                        best_w = cw[i];
+                        best_b = cb[j];
+                        best_p = f;
+                    }
                 }
-            }
+        b->persistent = best_p;
+        b->pblocks = 0;
         if (rc == XF_OK) rc = build_lists(b, best_w, best_b);
         for (int i = 0; i < n && rc == XF_OK; ++i) {
             std::vector<double> psi;
@@ -568,10 +579,10 @@ int xf_batch_tile_shape(const xf_batch* b, int* warps, double* tuned_ms)
 {
     if (!b) return XF_EINVAL;
     if (warps) *warps = b->warps;
-    // the one-beam-per-warp candidates {2, 4, 8} warps
+    // the graph-launched one-beam-per-warp candidates {2, 4, 8} warps
     if (tuned_ms)
         for (int i = 0, k = 0; i < b->ncand && k < 3; ++i)
-            if (b->cand_bpw[i] == 1) tuned_ms[k++] = b->cand_ms[i];
+            if (b->cand_bpw[i] == 1 && !b->cand_pers[i]) tuned_ms[k++] = b->cand_ms[i];
     return XF_OK;
 }
 
@@ -591,16 +602,18 @@ int xf_batch_set_persistent(xf_batch* b, int on, int beams_per_warp)
     return on ? build_lists(b, 8, beams_per_warp) : XF_OK;
 }
 
-int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* ncand, int* cand_warps, int* cand_bpw,
-                    double* cand_ms)
+int xf_batch_tuning(const xf_batch* b, int* warps, int* beams_per_warp, int* persistent, int* ncand, int* cand_warps,
+                    int* cand_bpw, int* cand_persistent, double* cand_ms)
 {
     if (!b) return XF_EINVAL;
     if (warps) *warps = b->warps;
     if (beams_per_warp) *beams_per_warp = b->bpw;
+    if (persistent) *persistent = b->persistent;
     if (ncand) *ncand = b->ncand;
     for (int i = 0; i < b->ncand; ++i) {
         if (cand_warps) cand_warps[i] = b->cand_warps[i];
         if (cand_bpw) cand_bpw[i] = b->cand_bpw[i];
+        if (cand_persistent) cand_persistent[i] = b->cand_pers[i];
         if (cand_ms) cand_ms[i] = b->cand_ms[i];
     }
     return XF_OK;

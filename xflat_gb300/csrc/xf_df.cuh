@@ -389,6 +389,17 @@ __device__ __forceinline__ void store_bin_raw(float* __restrict__ p, const DF4& 
 
 __device__ __forceinline__ void store_bin(float* __restrict__ p, const DF4& x) { store_bin_raw(p, norm4(x)); }
 
+// Intermediate states (psi1, psi3 and the halved psi4, read within the same
+// iteration): stored renormalised, or as computed with XF_DF_LOOSE_STORES.
+#ifndef XF_DF_LOOSE_STORES
+#define XF_DF_LOOSE_STORES 0
+#endif
+__device__ __forceinline__ void store_mid_bin(float* __restrict__ p, const DF4& x)
+{
+    if (XF_DF_LOOSE_STORES) store_bin_raw(p, x);
+    else store_bin(p, x);
+}
+
 __device__ __forceinline__ void prefetch_bin(const float* p)
 {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -450,8 +461,8 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
             const DF4 w = dsig_w(a00, a01, g01i, x);
             const DF4 y1 = dapply(.5f, k1, x, w);
             const DF4 y3 = dapply(1.f, k0, x, w);
-            store_bin(bin_ptr(d.psi1, epad, b, e), y1);
-            store_bin(bin_ptr(d.psi3, epad, b, e), y3);
+            store_mid_bin(bin_ptr(d.psi1, epad, b, e), y1);
+            store_mid_bin(bin_ptr(d.psi3, epad, b, e), y3);
             const DF f = fv_df(d, bi.p, e);
             dacc_rho(y1, f, v[0], v[1], v[2]);
             dacc_rho(y3, f, v[3], v[4], v[5]);
@@ -526,12 +537,13 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const DK ka = dcoeffs<1>(a00, a01, ga2, bl);
             const DF4 ya = dapply_z(.5f, ka, a00, a01, g101i, x);
             float* p1p = bin_ptr(d.psi1, epad, b, e);
-            store_bin(p1p, dadd4(ya, load_bin(p1p)));
+            store_mid_bin(p1p, dadd4(ya, load_bin(p1p)));
             // S8, stored halved for the average of S10/S11
             const DF b00 = ladd(hv0, g300), b01 = ladd(hv1, g301r);
             const DK kb = dcoeffs<1>(b00, b01, gb2, bl);
             const DF4 y4 = dapply_z(.5f, kb, b00, b01, g301i, x);
-            store_df(h4 + base, l4 + base, epad, e, y4);
+            if (XF_DF_LOOSE_STORES) store_raw(h4 + base, l4 + base, epad, e, y4);
+            else store_df(h4 + base, l4 + base, epad, e, y4);
             dacc_rho(y4, fv_df(d, bi.p, e), v[0], v[1], v[2]);
         }
         // psi4 was accumulated halved: its sums are a quarter (exactly) of psi4's
