@@ -92,7 +92,7 @@ def test_command_line_driver(tmp_path):
     assert out2.returncode == 0 and "Provided data file" in out2.stdout
 
 
-@pytest.mark.parametrize("precision,iters", [("fp64", 40), ("mixed", 30)])
+@pytest.mark.parametrize("precision,iters", [("fp64", 40), ("mixed", 30), ("df", 30)])
 def test_async_records_equal_states_of_each_accepted_step(tmp_path, precision, iters):
     """Every accepted step is dumped; the asynchronous copies and the writer
     thread must deliver, in order, exactly the state and survival of each
@@ -153,7 +153,8 @@ def _files(tmp_path, text, device, iters, k=5):
 
 
 @pytest.mark.parametrize("base,precision", [("config0_ma.txt", "fp64"), ("config0_ma.txt", "mixed"),
-                                            ("config3_maa.txt", "fp64"), ("config3_maa.txt", "mixed")])
+                                            ("config0_ma.txt", "df"), ("config3_maa.txt", "fp64"),
+                                            ("config3_maa.txt", "mixed"), ("config3_maa.txt", "df")])
 def test_device_control_writes_the_host_loops_files(tmp_path, base, precision):
     """Under device control the step controller evaluates the dump triggers
     and phase A stages the records: the files equal, record for record, those

@@ -328,6 +328,20 @@ __device__ __forceinline__ double byte_reversed(double v)
 // with the spectrum of particle p % 2 (src/IO_f.cpp:341-351), reduced in the
 // order of the stand-alone output kernels so both routes write the same
 // bits.  psi is the FP64 state, or null for the compensated pair (hi, lo).
+// Component k of energy bin e of beam b of a compensated-pair state (hi, lo)
+// as a double: the mixed path's rows ([beam][comp][epad] hi and lo arrays)
+// or, for the double-float path (d.df), its bin layout ([beam][epad][8]
+// floats in the buffer at hi: the four hi parts, then the four lo parts).
+__device__ __forceinline__ double pair_at(const Dev& d, const float* hi, const float* lo, int b, int k, int e)
+{
+    if (d.df) {
+        const float* p = hi + ((size_t)b * d.epad + e) * 8;
+        return (double)p[k] + (double)p[4 + k];
+    }
+    const size_t i = ((size_t)b * 4 + k) * d.epad + e;
+    return (double)hi[i] + (double)lo[i];
+}
+
 __device__ inline void stage_beam(const Dev& d, const Ctl* ctl, int kind, int b, int lane, const double* psi,
                                   const float* hi, const float* lo)
 {
@@ -337,8 +351,7 @@ __device__ inline void stage_beam(const Dev& d, const Ctl* ctl, int kind, int b,
         double* dst = ctl->io_snap + (size_t)ctl->stage_snap_slot * ((size_t)d.nbeams * 4 * ne) + (size_t)b * 4 * ne;
         for (int k = 0; k < 4; ++k)
             for (int e = lane; e < ne; e += 32) {
-                const size_t i = base + (size_t)k * epad + e;
-                const double v = psi ? psi[i] : (double)hi[i] + (double)lo[i];
+                const double v = psi ? psi[base + (size_t)k * epad + e] : pair_at(d, hi, lo, b, k, e);
                 dst[(size_t)k * ne + e] = byte_reversed(v);
             }
     }
@@ -351,8 +364,8 @@ __device__ inline void stage_beam(const Dev& d, const Ctl* ctl, int kind, int b,
                 ar = psi[base + e];
                 ai = psi[base + epad + e];
             } else {
-                ar = (double)hi[base + e] + (double)lo[base + e];
-                ai = (double)hi[base + epad + e] + (double)lo[base + epad + e];
+                ar = pair_at(d, hi, lo, b, 0, e);
+                ai = pair_at(d, hi, lo, b, 1, e);
             }
             s = fma(ar * ar + ai * ai, fv[e], s);
         }

@@ -33,9 +33,10 @@
 // offset, once per beam, lane-parallel) and split into pairs; the vacuum
 // term, energy weights and path lengths come from pair tables.  Moments are
 // accumulated in pairs, scaled by kappa (add_moment_df), and reduced across
-// blocks in FP64.  psi0 and the candidate share the mixed path's
-// compensated-pair buffers; psi1 and psi3 are pairs stored bin by bin in the
-// FP64 path's buffers (bin_ptr).
+// blocks in FP64.  Every state is stored bin by bin ([beam][ebin][8] floats:
+// the four components' hi parts, then their lo parts), psi0 and the candidate
+// in the pair buffers the mixed path uses for its rows (sbin_ptr), psi1 and
+// psi3 in the FP64 path's buffers (bin_ptr).
 #pragma once
 #include "xf_mixed.cuh"
 
@@ -132,16 +133,6 @@ struct DF4 {
     DF ar, ai, br, bi;
 };
 
-__device__ __forceinline__ DF4 load_df(const float* __restrict__ hi, const float* __restrict__ lo, int epad, int e)
-{
-    DF4 x;
-    x.ar = DF{hi[e], lo[e]};
-    x.ai = DF{hi[epad + e], lo[epad + e]};
-    x.br = DF{hi[2 * epad + e], lo[2 * epad + e]};
-    x.bi = DF{hi[3 * epad + e], lo[3 * epad + e]};
-    return x;
-}
-
 __device__ __forceinline__ DF4 norm4(const DF4& x)
 {
     DF4 y;
@@ -150,33 +141,6 @@ __device__ __forceinline__ DF4 norm4(const DF4& x)
     y.br = norm(x.br);
     y.bi = norm(x.bi);
     return y;
-}
-
-// Stores a renormalised x.
-__device__ __forceinline__ void store_raw(float* __restrict__ hi, float* __restrict__ lo, int epad, int e, const DF4& x)
-{
-    hi[e] = x.ar.h;
-    lo[e] = x.ar.l;
-    hi[epad + e] = x.ai.h;
-    lo[epad + e] = x.ai.l;
-    hi[2 * epad + e] = x.br.h;
-    lo[2 * epad + e] = x.br.l;
-    hi[3 * epad + e] = x.bi.h;
-    lo[3 * epad + e] = x.bi.l;
-}
-
-// Stores x renormalised.
-__device__ __forceinline__ void store_df(float* __restrict__ hi, float* __restrict__ lo, int epad, int e, const DF4& x)
-{
-    store_raw(hi, lo, epad, e, norm4(x));
-}
-
-__device__ __forceinline__ void prefetch_rows(const float* b, int epad, int e)
-{
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + e));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + epad + e));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + 2 * epad + e));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(b + 3 * epad + e));
 }
 
 // ------------------------------------------------------------------ propagators
@@ -273,7 +237,7 @@ __device__ __forceinline__ DF4 dsig_w(const DF& h00, const DF& h01r, const DF& h
     return w;
 }
 
-// y = U x = q x + cm x + S w (loose; store_df renormalises).
+// y = U x = q x + cm x + S w (loose; the stores renormalise).
 __device__ __forceinline__ DF4 dapply(float q, const DK& k, const DF4& x, const DF4& w)
 {
     DF4 y;
@@ -400,6 +364,17 @@ __device__ __forceinline__ void store_mid_bin(float* __restrict__ p, const DF4& 
     else store_bin(p, x);
 }
 
+// psi0 and the candidate: the same bin layout in their own buffers
+// (pair_at in xf_common.cuh reads it for the output and sum kernels).
+__device__ __forceinline__ float* sbin_ptr(float* buf, int epad, int b, int e)
+{
+    return buf + ((size_t)b * epad + e) * 8;
+}
+__device__ __forceinline__ const float* sbin_ptr(const float* buf, int epad, int b, int e)
+{
+    return buf + ((size_t)b * epad + e) * 8;
+}
+
 __device__ __forceinline__ void prefetch_bin(const float* p)
 {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -415,8 +390,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
     if (ctl->done) return;
     __shared__ double s_warp[8 * 32];
     __shared__ double s_out[32];
-    const float* __restrict__ h0 = ctl->m0hi;
-    const float* __restrict__ l0 = ctl->m0lo;
+    const float* __restrict__ s0 = ctl->m0hi;
     const double hm = ctl->hm[0];
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
@@ -437,17 +411,15 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
         const DLen bm0 = dlen(shfl_df(sv, 3));
         DLen bm1;
         if (GEOM == 1) bm1 = dlen(shfl_df(sv, 4));
-        const size_t base = (size_t)b * 4 * epad;
         DF v[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) v[i] = DF{0.f, 0.f};
         for (int e = lane; e < epad; e += 32) {
             if (pf && e + pf < epad) {
-                prefetch_rows(h0 + base, epad, e + pf);
-                prefetch_rows(l0 + base, epad, e + pf);
+                prefetch_bin(sbin_ptr(s0, epad, b, e + pf));
             }
             const DF a00 = ladd(hv_df(d, 0, e), g00), a01 = ladd(hv_df(d, 1, e), g01r);
-            const DF4 x = load_df(h0 + base, l0 + base, epad, e);
+            const DF4 x = load_bin(sbin_ptr(s0, epad, b, e));
             const DK k0 = dcoeffs<0>(a00, a01, g01i2, bm0);
             DK k1;
             if (GEOM == 0) {
@@ -500,10 +472,8 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
     if (ctl->done) return;
     __shared__ double s_warp[8 * 32];
     __shared__ double s_out[32];
-    const float* __restrict__ h0 = ctl->m0hi;
-    const float* __restrict__ l0 = ctl->m0lo;
-    float* h4 = ctl->m4hi;
-    float* l4 = ctl->m4lo;
+    const float* __restrict__ s0 = ctl->m0hi;
+    float* s4 = ctl->m4hi;
     const double hm_rdr = ctl->hm[2], hm_rdr2 = ctl->hm[1];
     const int lane = threadIdx.x & 31;
     const int gw = first + (threadIdx.x >> 5), tw = stride;
@@ -522,16 +492,14 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
         const DF g300 = shfl_df(sv, 3), g301r = shfl_df(sv, 4), g301i = shfl_df(sv, 5);
         const DLen bl = dlen(shfl_df(sv, 6));
         const DF ga2 = dsq(g101i), gb2 = dsq(g301i);
-        const size_t base = (size_t)b * 4 * epad;
         DF v[4] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
         for (int e = lane; e < epad; e += 32) {
             if (pf && e + pf < epad) {
-                prefetch_rows(h0 + base, epad, e + pf);
-                prefetch_rows(l0 + base, epad, e + pf);
+                prefetch_bin(sbin_ptr(s0, epad, b, e + pf));
                 prefetch_bin(bin_ptr(d.psi1, epad, b, e + pf));
             }
             const DF hv0 = hv_df(d, 0, e), hv1 = hv_df(d, 1, e);
-            const DF4 x = load_df(h0 + base, l0 + base, epad, e);
+            const DF4 x = load_bin(sbin_ptr(s0, epad, b, e));
             // S4/S5: (U psi0 + psi1)/2 as U/2 psi0 + psi1/2 (psi1 stored halved by phase A)
             const DF a00 = ladd(hv0, g100), a01 = ladd(hv1, g101r);
             const DK ka = dcoeffs<1>(a00, a01, ga2, bl);
@@ -542,8 +510,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
             const DF b00 = ladd(hv0, g300), b01 = ladd(hv1, g301r);
             const DK kb = dcoeffs<1>(b00, b01, gb2, bl);
             const DF4 y4 = dapply_z(.5f, kb, b00, b01, g301i, x);
-            if (XF_DF_LOOSE_STORES) store_raw(h4 + base, l4 + base, epad, e, y4);
-            else store_df(h4 + base, l4 + base, epad, e, y4);
+            store_mid_bin(sbin_ptr(s4, epad, b, e), y4);
             dacc_rho(y4, fv_df(d, bi.p, e), v[0], v[1], v[2]);
         }
         // psi4 was accumulated halved: its sums are a quarter (exactly) of psi4's
@@ -572,8 +539,7 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
     if (ctl->done) return;
     __shared__ double s_warp[8 * 32];
     __shared__ double s_out[32];
-    float* h4 = ctl->m4hi;
-    float* l4 = ctl->m4lo;
+    float* s4 = ctl->m4hi;
     double* __restrict__ S4 = ctl->S4;
     float2* __restrict__ S4f = ctl->S4f;
     const double hm_rdr = ctl->hm[2];
@@ -593,14 +559,12 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
         const DF g00 = shfl_df(sv, 0), g01r = shfl_df(sv, 1), g01i = shfl_df(sv, 2);
         const DLen bm = dlen(shfl_df(sv, 3));
         const DF g01i2 = dsq(g01i);
-        const size_t base = (size_t)b * 4 * epad;
         DF v[4] = {DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}, DF{0.f, 0.f}};
         float err = 0.f;
         for (int e = lane; e < epad; e += 32) {
             if (pf && e + pf < epad) {
                 prefetch_bin(bin_ptr(d.psi3, epad, b, e + pf));
-                prefetch_rows(h4 + base, epad, e + pf);
-                prefetch_rows(l4 + base, epad, e + pf);
+                prefetch_bin(sbin_ptr(s4, epad, b, e + pf));
                 prefetch_bin(bin_ptr(d.psi1, epad, b, e + pf));
             }
             const DF a00 = ladd(hv_df(d, 0, e), g00), a01 = ladd(hv_df(d, 1, e), g01r);
@@ -608,8 +572,9 @@ __device__ inline void phaseC_body(const Dev& d, int first, int stride, const Re
             // S10/S11: (U psi3 + psi4)/2 as U/2 psi3 + psi4/2 (psi4 stored halved by phase B)
             const DK k = dcoeffs<1>(a00, a01, g01i2, bm);
             const DF4 y3 = dapply_z(.5f, k, a00, a01, g01i, x3);
-            const DF4 c = norm4(dadd4(y3, load_df(h4 + base, l4 + base, epad, e)));
-            store_raw(h4 + base, l4 + base, epad, e, c);
+            float* cp = sbin_ptr(s4, epad, b, e);
+            const DF4 c = norm4(dadd4(y3, load_bin(cp)));
+            store_bin_raw(cp, c);
             // calcErrHvv against psi1: the hi parts of two states this close
             // differ exactly (Sterbenz), so the difference is exact to 2^-48
             // of the state, far below the error's own size

@@ -164,7 +164,8 @@ __global__ void k_stage_state(Dev d, int mixed, int big_endian, double* __restri
     const float* __restrict__ lo = ctl->m0lo;
     const double* __restrict__ src = ctl->psi0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double v = mixed ? (double)hi[i] + (double)lo[i] : src[i];
+        const size_t r = i / d.epad;
+        const double v = mixed ? pair_at(d, hi, lo, (int)(r / 4), (int)(r % 4), (int)(i - r * d.epad)) : src[i];
         dst[i] = big_endian ? byte_reversed(v) : v;
     }
 }
@@ -184,8 +185,8 @@ __global__ void k_survival(Dev d, int mixed, double* __restrict__ out)
         for (int e = lane; e < epad; e += 32) {
             double ar, ai;
             if (mixed) {
-                ar = (double)ctl->m0hi[base + e] + (double)ctl->m0lo[base + e];
-                ai = (double)ctl->m0hi[base + epad + e] + (double)ctl->m0lo[base + epad + e];
+                ar = pair_at(d, ctl->m0hi, ctl->m0lo, b, 0, e);
+                ai = pair_at(d, ctl->m0hi, ctl->m0lo, b, 1, e);
             } else {
                 ar = ctl->psi0[base + e];
                 ai = ctl->psi0[base + epad + e];

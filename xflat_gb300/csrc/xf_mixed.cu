@@ -137,10 +137,21 @@ Mixed* mixed_create(xf_handle* h)
 {
     Mixed* m = new Mixed();
     const size_t n = (size_t)h->nbeams * 4 * h->epad;
+    const bool df = h->cfg.precision == XF_PREC_DF;
     bool ok = true;
     for (int i = 0; i < 2 && ok; ++i) {
-        ok = ok && cudaMalloc(&m->hi[i], n * sizeof(float)) == cudaSuccess && cudaMemset(m->hi[i], 0, n * sizeof(float)) == cudaSuccess;
-        ok = ok && cudaMalloc(&m->lo[i], n * sizeof(float)) == cudaSuccess && cudaMemset(m->lo[i], 0, n * sizeof(float)) == cudaSuccess;
+        if (df) {
+            // double-float: one buffer in the bin layout ([beam][epad][8] floats,
+            // pair_at); lo points at its second half and is not read on its own
+            ok = ok && cudaMalloc(&m->hi[i], 2 * n * sizeof(float)) == cudaSuccess &&
+                 cudaMemset(m->hi[i], 0, 2 * n * sizeof(float)) == cudaSuccess;
+            if (ok) m->lo[i] = m->hi[i] + n;
+        } else {
+            ok = ok && cudaMalloc(&m->hi[i], n * sizeof(float)) == cudaSuccess &&
+                 cudaMemset(m->hi[i], 0, n * sizeof(float)) == cudaSuccess;
+            ok = ok && cudaMalloc(&m->lo[i], n * sizeof(float)) == cudaSuccess &&
+                 cudaMemset(m->lo[i], 0, n * sizeof(float)) == cudaSuccess;
+        }
         ok = ok && cudaMalloc(&m->S[i], 4 * (size_t)h->nbeams * sizeof(double)) == cudaSuccess;
         ok = ok && cudaMalloc(&m->Sf[i], 4 * (size_t)h->nbeams * sizeof(float2)) == cudaSuccess &&
              cudaMemset(m->Sf[i], 0, 4 * (size_t)h->nbeams * sizeof(float2)) == cudaSuccess;
@@ -196,8 +207,9 @@ void mixed_destroy(Mixed* m)
 {
     if (!m) return;
     for (int i = 0; i < 2; ++i) {
+        const bool shared = m->lo[i] && m->hi[i] && m->lo[i] > m->hi[i];  // double-float: lo inside hi's buffer
         if (m->hi[i]) cudaFree(m->hi[i]);
-        if (m->lo[i]) cudaFree(m->lo[i]);
+        if (m->lo[i] && !shared) cudaFree(m->lo[i]);
         if (m->S[i]) cudaFree(m->S[i]);
         if (m->Sf[i]) cudaFree(m->Sf[i]);
     }
@@ -214,16 +226,30 @@ int mixed_set_state(xf_handle* h, Mixed* m, const double* psi)
     int rc;
     if ((rc = h->pull_ctl())) return rc;
     const size_t n = (size_t)h->nbeams * 4 * h->epad;
-    std::vector<float> hi(n, 0.f), lo(n, 0.f);
-    for (size_t r = 0; r < (size_t)h->nbeams * 4; ++r)
-        for (int e = 0; e < h->ne; ++e) {
-            const double x = psi[r * h->ne + e];
-            const float xh = (float)x;
-            hi[r * h->epad + e] = xh;
-            lo[r * h->epad + e] = (float)(x - (double)xh);
-        }
-    XM_CUDA(h, cudaMemcpy(h->h_ctl->m0hi, hi.data(), n * sizeof(float), cudaMemcpyHostToDevice));
-    XM_CUDA(h, cudaMemcpy(h->h_ctl->m0lo, lo.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    if (h->dev.df) {
+        // bin layout: [beam][epad][hi0..hi3, lo0..lo3]
+        std::vector<float> bins(2 * n, 0.f);
+        for (size_t r = 0; r < (size_t)h->nbeams * 4; ++r)
+            for (int e = 0; e < h->ne; ++e) {
+                const double x = psi[r * h->ne + e];
+                const float xh = (float)x;
+                float* p = &bins[((r / 4) * h->epad + e) * 8];
+                p[r % 4] = xh;
+                p[4 + r % 4] = (float)(x - (double)xh);
+            }
+        XM_CUDA(h, cudaMemcpy(h->h_ctl->m0hi, bins.data(), 2 * n * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> hi(n, 0.f), lo(n, 0.f);
+        for (size_t r = 0; r < (size_t)h->nbeams * 4; ++r)
+            for (int e = 0; e < h->ne; ++e) {
+                const double x = psi[r * h->ne + e];
+                const float xh = (float)x;
+                hi[r * h->epad + e] = xh;
+                lo[r * h->epad + e] = (float)(x - (double)xh);
+            }
+        XM_CUDA(h, cudaMemcpy(h->h_ctl->m0hi, hi.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        XM_CUDA(h, cudaMemcpy(h->h_ctl->m0lo, lo.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    }
     k_mix_esum<<<max_phase_blocks(h->nbeams, 256), 256, 0, h->st>>>(h->dev, 0, 0);
     XM_CUDA(h, cudaGetLastError());
     XM_CUDA(h, cudaStreamSynchronize(h->st));
@@ -238,6 +264,17 @@ int mixed_get_state(xf_handle* h, Mixed* m, int which, double* psi)
     int rc;
     if ((rc = h->pull_ctl())) return rc;
     const size_t n = (size_t)h->nbeams * 4 * h->epad;
+    if (h->dev.df) {
+        std::vector<float> bins(2 * n);
+        XM_CUDA(h, cudaMemcpy(bins.data(), which == 0 ? h->h_ctl->m0hi : h->h_ctl->m4hi, 2 * n * sizeof(float),
+                              cudaMemcpyDeviceToHost));
+        for (size_t r = 0; r < (size_t)h->nbeams * 4; ++r)
+            for (int e = 0; e < h->ne; ++e) {
+                const float* p = &bins[((r / 4) * h->epad + e) * 8];
+                psi[r * h->ne + e] = (double)p[r % 4] + (double)p[4 + r % 4];
+            }
+        return XF_OK;
+    }
     std::vector<float> hi(n), lo(n);
     XM_CUDA(h, cudaMemcpy(hi.data(), which == 0 ? h->h_ctl->m0hi : h->h_ctl->m4hi, n * sizeof(float), cudaMemcpyDeviceToHost));
     XM_CUDA(h, cudaMemcpy(lo.data(), which == 0 ? h->h_ctl->m0lo : h->h_ctl->m4lo, n * sizeof(float), cudaMemcpyDeviceToHost));

@@ -818,7 +818,7 @@ __device__ inline void esum_body(const Dev& d, int first, int stride, int renorm
             for (int e = lane; e < epad; e += 32) {
                 double a[4];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) a[k] = (double)ph[k * epad + e] + (double)pl[k * epad + e];
+                for (int k = 0; k < 4; ++k) a[k] = pair_at(d, hi, lo, b, k, e);
                 const double fe = fvp[e];
                 v[1] = fma((a[0] * a[0] + a[1] * a[1]) - (a[2] * a[2] + a[3] * a[3]), fe, v[1]);
                 v[2] = fma(a[0] * a[2] + a[1] * a[3], fe, v[2]);
