@@ -154,8 +154,9 @@ int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins)
  * iterations, the stages separated by grid barriers whose waits are bounded
  * by "barrier_timeout_ms" (default 2000; XF_ETIMEOUT when one runs out;
  * "debug_barrier_extra" > 0 makes every wait run out, for tests), not when
- * time_phases is set; "fp64_fused" = 1 folds the FP64 averages of phases B
- * and C into their FMA chains (other rounding); "debug_psi3" = 1 makes the last
+ * time_phases is set; "fp64_fused" (default 1) folds the FP64 averages of
+ * phases B and C into their FMA chains, 0 keeps them as separate additions
+ * (other rounding; graph-launched only); "debug_psi3" = 1 makes the last
  * phase also store U(h4, dl2) psi3 into psi3, as the reference's in-place
  * stage S10 does (src/Nmr.cpp:191). */
 int xf_set_option(xf_handle* h, const char* name, double value);

@@ -587,12 +587,14 @@ int xf_handle::run_device(const xf_run_opts& o, xf_run_stats& s)
     }
     const bool files = o.write_files && cfg.dump_mode != 0;
     // the persistent loop serves FP64 and double-float; per-phase timing needs the graphs' events.
-    // Measured on GB300 (ms per iteration, graphs -> persistent): double-float 0.0512 -> 0.0500 at
-    // 65 K bins, 0.109 -> 0.102 at 524 K, 0.502 -> 0.483 at 4.19 M; FP64 0.0734 -> 0.0679 at 65 K,
-    // 0.280 -> 0.284 at 524 K, 1.70 -> 1.91 at 4.19 M.  The default takes it for double-float, and
-    // for FP64 when one wave of two 8-warp blocks per SM covers every beam.
-    const bool auto_pers = dev.df || (!mixed && nbeams <= 2 * 152 * 8);
-    const bool pers = (persistent > 0 || (persistent < 0 && auto_pers)) && (!mixed || dev.df) && !o.time_phases;
+    // The default takes it when one wave of two 8-warp blocks per SM covers every beam: there it
+    // wins (GB300, ms per iteration, graphs -> persistent, 65 K bins: FP64 0.0734 -> 0.0679,
+    // double-float 0.0512 -> 0.0500), while at 4.19 M bins the phase kernels' own grids are
+    // better balanced (FP64 1.70 -> 1.91, double-float 0.442 -> 0.465).
+    const bool auto_pers = (!mixed || dev.df) && nbeams <= 2 * 152 * 8;
+    // (the persistent kernel has the FP64 averages folded; fp64_fused = 0 runs the graphs)
+    const bool pers = (persistent > 0 || (persistent < 0 && auto_pers)) && (!mixed || dev.df) && !o.time_phases &&
+                      (dev.df || shape.fp64_fused);
     if (files && (rc = io_dev_prepare(k))) return rc;
     if ((rc = start_device_run(r, dr, Ts, files))) return rc;
     // instantiate the graph sizes this run needs before the timed region starts

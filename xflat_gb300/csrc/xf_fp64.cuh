@@ -273,7 +273,7 @@ __device__ inline void phaseA_body(const Dev& d, int first, int stride, const Re
 
 // S4/S5 (psi4' = U(h1, dl1, hm(r+dr)) psi0 averaged into psi1) and S8
 // (psi4 = U(h3, dl1, hm(r+dr/2)) psi0) with the moments of psi4 at point 2 (S9).
-template <int GEOM, int FUSE = 0>
+template <int GEOM, int FUSE = 1>
 __device__ inline void phaseB_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
@@ -353,7 +353,7 @@ __device__ inline void phaseB_body(const Dev& d, int first, int stride, const Re
 // max over beams (src/Nmr.cpp:195-206), and the moments of the candidate.
 // Under device control the last block also runs the step controller of
 // src/Nmr.cpp:227-249.
-template <int GEOM, int FUSE = 0>
+template <int GEOM, int FUSE = 1>
 __device__ inline void phaseC_body(const Dev& d, int first, int stride, const RedTarget& rt, int end = -1)
 {
     constexpr int K = NK<GEOM>::K;
