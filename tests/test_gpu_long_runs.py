@@ -16,7 +16,8 @@ one FP64 batch, compared the same way at 600 km.
 Bars: double-float within 1e-5 of FP64 (the spec bar); mixed precision
 is recorded, not asserted (it is not expected to hold 1e-5 through long runs:
 see tests/test_gpu_full_run.py).  Set XF_LONG_RUNS=1 to run (about 20
-GPU-minutes); XF_LONG_RUNS_OUT=<file> saves the numbers as JSON."""
+GPU-minutes); XF_LONG_RUNS_OUT=<file> saves the numbers as JSON;
+XF_LONG_RUNS_ONLY (comma-separated: inverted, normal, batch) selects parts."""
 import json
 import os
 
@@ -31,6 +32,12 @@ pytestmark = [pytest.mark.gpu,
                                  reason="runs to 1500 km take ~20 GPU-minutes: set XF_LONG_RUNS=1")]
 
 RESULTS = {}
+ONLY = [x for x in os.environ.get("XF_LONG_RUNS_ONLY", "").split(",") if x]
+
+
+def _selected(part):
+    if ONLY and part not in ONLY:
+        pytest.skip("not selected by XF_LONG_RUNS_ONLY")
 
 
 def pee(psi):
@@ -47,6 +54,7 @@ def _save():
 
 @pytest.mark.parametrize("hierarchy,dm2", [("inverted", "-3E-3"), ("normal", "3E-3")])
 def test_config2_to_1500km(hierarchy, dm2):
+    _selected(hierarchy)
     runs = {}
     for prec in ("fp64", "df", "mixed"):
         text = derive("config1_ma.txt", R0=50, dr="1.5e-4", Rn=1500, dm2=dm2, precision=prec)
@@ -68,6 +76,7 @@ def test_config2_to_1500km(hierarchy, dm2):
 
 
 def test_batched_sweep_subset_to_600km():
+    _selected("batch")
     from xflat_gb300.sweep import sweep_configs
     sizes = [xg.Config.from_text(t) for t in sweep_configs(seed=4, n=64)]
     pick = sorted(range(64), key=lambda i: sizes[i].abins * sizes[i].ebins)[:8]

@@ -57,11 +57,12 @@ constexpr long long kT3 = 0x3F50624DD2F1A9FCLL;  // 1e-3
 constexpr long long kT4 = 0x3F847AE147AE147BLL;  // 1e-2
 
 // Per-beam constants of one propagator: h01i (not energy dependent) squared,
-// dl^2, and the degree-2 sinc polynomial's coefficients times dl, so that the
-// common branch of su2_coeffs costs 2 + 1 + 2 + 2 FP64 operations per bin.
+// dl^2, and the sinc polynomial's first coefficients times dl, so that the
+// degree-2 and degree-3 branches of su2_coeffs need no multiplication by dl
+// per bin (2 + 1 + 2 + 2 and 2 + 1 + 3 + 3 FP64 operations).
 struct PropK {
     double dl, dl2, h01i2;
-    double s0, s1, s2;  // q dl (1, -1/6, 1/120)
+    double s0, s1, s2, s3;  // q dl (1, -1/6, 1/120, -1/5040)
 };
 
 template <int Q2 = 0>
@@ -75,6 +76,7 @@ __device__ __forceinline__ PropK prop_k(double h01i, double dl)
     p.s0 = q * dl;
     p.s1 = (q * (-1.0 / 6.0)) * dl;
     p.s2 = (q * (1.0 / 120.0)) * dl;
+    p.s3 = (q * (-1.0 / 5040.0)) * dl;
     return p;
 }
 
@@ -91,7 +93,7 @@ __device__ __forceinline__ void su2_coeffs(double h00, double h01r, const PropK&
         S = fma(fma(t, pk.s2, pk.s1), t, pk.s0);
     } else if (__all_sync(kFull, tb <= kT3)) {
         C = fma(fma(fma(t, q * (-1.0 / 720.0), q * (1.0 / 24.0)), t, q * -0.5), t, q);
-        S = fma(fma(fma(t, q * (-1.0 / 5040.0), q * (1.0 / 120.0)), t, q * (-1.0 / 6.0)), t, q) * dl;
+        S = fma(fma(fma(t, pk.s3, pk.s2), t, pk.s1), t, pk.s0);
     } else if (__all_sync(kFull, tb <= kT4)) {
         C = fma(fma(fma(fma(t, q * (1.0 / 40320.0), q * (-1.0 / 720.0)), t, q * (1.0 / 24.0)), t, q * -0.5), t, q);
         S = fma(fma(fma(fma(t, q * (1.0 / 362880.0), q * (-1.0 / 5040.0)), t, q * (1.0 / 120.0)), t, q * (-1.0 / 6.0)),
