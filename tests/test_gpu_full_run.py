@@ -7,7 +7,7 @@ about 1.1e7 stepper iterations, free-running under device control.
   the reference built from its sources): the same final radius, and P_ee(E)
   of every nu_e beam within 1e-6 (absolute).  Measured on a GB300 against the
   reference's run (20,450 s on 8 cores): the same 11,161,528 iterations and
-  11,161,483 accepted steps, max 7.6e-7 (median 3.1e-8).  The accepted-step
+  11,161,483 accepted steps, max 9.1e-7 (median 3.2e-8).  The accepted-step
   counts are recorded, not compared: the last bits of the moment sums differ
   (another summation order), and over 1e7 adaptive steps that may move a
   decision.
@@ -23,7 +23,7 @@ about 1.1e7 stepper iterations, free-running under device control.
 - Double-float against FP64 at 300 km: P_ee(E) within 1e-5.  Its per-step
   rounding is about 30 times FP64's (pairs of FP32 carry about 48 bits),
   which the amplification above turns into a few 1e-6: measured on a GB300,
-  the same 11,161,528 iterations and accepted steps as FP64, max 3.7e-6
+  the same 11,161,528 iterations and accepted steps as FP64, max 3.5e-6
   (median 1.6e-7), per-beam survival 6.2e-7.
 
 It takes about 21 minutes on a GB300 for FP64 and double-float (the mixed run adds
