@@ -354,26 +354,9 @@ __device__ __forceinline__ void store_bin_raw(float* __restrict__ p, const DF4& 
 __device__ __forceinline__ void store_bin(float* __restrict__ p, const DF4& x) { store_bin_raw(p, norm4(x)); }
 
 // Intermediate states (psi1, psi3 and the halved psi4, read within the same
-// iteration): stored renormalised, or as computed with XF_DF_LOOSE_STORES.
-#ifndef XF_DF_LOOSE_STORES
-#define XF_DF_LOOSE_STORES 0
-#endif
-__device__ __forceinline__ void store_mid_bin(float* __restrict__ p, const DF4& x)
-{
-    if (XF_DF_LOOSE_STORES) store_bin_raw(p, x);
-    else store_bin(p, x);
-}
-
-// psi0 and the candidate: the same bin layout in their own buffers
-// (pair_at in xf_common.cuh reads it for the output and sum kernels).
-__device__ __forceinline__ float* sbin_ptr(float* buf, int epad, int b, int e)
-{
-    return buf + ((size_t)b * epad + e) * 8;
-}
-__device__ __forceinline__ const float* sbin_ptr(const float* buf, int epad, int b, int e)
-{
-    return buf + ((size_t)b * epad + e) * 8;
-}
+// iteration) are stored renormalised as well: storing them as computed saved
+// 0.6 % on GB300, not worth the looser pairs.
+__device__ __forceinline__ void store_mid_bin(float* __restrict__ p, const DF4& x) { store_bin(p, x); }
 
 __device__ __forceinline__ void prefetch_bin(const float* p)
 {
