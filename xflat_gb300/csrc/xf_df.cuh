@@ -358,6 +358,17 @@ __device__ __forceinline__ void store_bin(float* __restrict__ p, const DF4& x) {
 // 0.6 % on GB300, not worth the looser pairs.
 __device__ __forceinline__ void store_mid_bin(float* __restrict__ p, const DF4& x) { store_bin(p, x); }
 
+// psi0 and the candidate: the same bin layout in their own buffers
+// (pair_at in xf_common.cuh reads it for the output and sum kernels).
+__device__ __forceinline__ float* sbin_ptr(float* buf, int epad, int b, int e)
+{
+    return buf + ((size_t)b * epad + e) * 8;
+}
+__device__ __forceinline__ const float* sbin_ptr(const float* buf, int epad, int b, int e)
+{
+    return buf + ((size_t)b * epad + e) * 8;
+}
+
 __device__ __forceinline__ void prefetch_bin(const float* p)
 {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
