@@ -233,6 +233,15 @@ int xf_calc_hvv_static(int geometry, int abins, int pbins, int ebins, int epad, 
  * blocks per SM) for about `ms` milliseconds: *tflops = 2 flops per FMA. */
 int xf_probe_fp64_peak(double ms, double* tflops);
 
+/* No reference counterpart.  The double-float propagator coefficients of
+ * NBeam::U (src/NBeam.cpp:360-393) for n bin Hamiltonians: h[3i..3i+2] =
+ * (h00, h01r, h01i) and path length dl[i] (host arrays), each split into FP32
+ * pairs, evaluated on the device by the double-float kernels' own code, with
+ * q = 1/2 when `half` is set, else 1.  Returns cm[i] = q (cos(|h| dl) - 1)
+ * and S[i] = q sin(|h| dl) / |h| (host arrays).  The series branch is chosen
+ * per warp of 32 consecutive inputs, as in the kernels. */
+int xf_probe_df_propagator(int n, const double* h, const double* dl, int half, double* cm, double* S);
+
 /* ---------------------------------------------------------------- files */
 /* The reference's NetCDF IO module (src/IO_f.cpp), written without libnetcdf
  * in the classic format (64-bit offsets): file names <prefix>Snapshot<n>_0_.nc

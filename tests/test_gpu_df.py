@@ -50,16 +50,62 @@ def test_replay_reference_step_sequence(name):
     assert err <= POL_TOL, err
 
 
-@pytest.mark.parametrize("r,dr", [(10.0, 1.3e-8), (20.0, 1.2e-5), (50.0, 1.5e-4), (200.0, 5e-3), (40.0, 0.05)])
-def test_one_iteration_vs_fp64(r, dr):
-    """Includes a step with t = |h|^2 dl^2 above 1e-3 (the pair Horner series)."""
+@pytest.mark.parametrize("r,dr,tol", [(10.0, 1.3e-8, 1e-13), (20.0, 1.2e-5, 1e-13), (50.0, 1.5e-4, 1e-13),
+                                      (200.0, 5e-3, 1e-13), (40.0, 0.05, 1e-13), (10.0, 1e-3, 1e-11)])
+def test_one_iteration_vs_fp64(r, dr, tol):
+    """Includes a step with t = |h|^2 dl^2 above 1e-3 (the pair Horner series)
+    and the first step of a run from 10 km (dl = 1e-3 km / cos, up to 0.06 km
+    in the outermost angle bin, across the matter and neutrino potentials at
+    the neutrinosphere: angles |h| dl far above 1 in most bins, the reduced
+    branch, whose pairs keep the angle to about 1e-14 of itself, so the state
+    bar grows with the largest angle; measured 2.6e-12 on a GB300).  The step
+    error, which is all a rejected first step passes on, stays within 1e-5 of
+    FP64's."""
     a, b = _pair(derive("config0_ma.txt", Abins=32, Ebins=64))
     me64 = a.step(r, dr)
     me2 = b.step(r, dr)
     assert abs(me2 - me64) <= 1e-5 * me64, (me2, me64)
     a.accept()
     b.accept()
-    assert np.max(np.abs(b.get_state(0) - a.get_state(0))) <= 1e-13
+    assert np.max(np.abs(b.get_state(0) - a.get_state(0))) <= tol
+
+
+def _pair_rounded(x):
+    """x as the double-float kernels see it: a hi FP32 part and an FP32 lo part."""
+    h = x.astype(np.float32).astype(np.float64)
+    return h + (x - h).astype(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize("half", [0, 1])
+def test_propagator_coefficients_every_branch(half):
+    """q (cos(|h| dl) - 1) and q sin(|h| dl) / |h| against numpy's FP64 sine
+    on the pair-rounded inputs, in each series branch (warps of 32 inputs):
+    the FP32 tail (t <= 1e-3), the pair Horner series (t <= 0.25) and the
+    reduced branch, with angles up to 2000 and next to multiples of pi/2.
+    The bar, 1e-14 + 4e-14 |h| dl, is the pairs' own precision of the angle
+    (about 1e-14 of it) with a margin of four."""
+    rng = np.random.default_rng(7 + half)
+    theta = np.concatenate([10.0 ** rng.uniform(-4, np.log10(0.03), 128),
+                            rng.uniform(0.04, 0.5, 128),
+                            10.0 ** rng.uniform(np.log10(0.51), np.log10(2000.0), 256),
+                            np.repeat(np.arange(1, 33) * np.pi / 2, 2) + np.tile([-1e-7, 1e-7], 32)])
+    lam = 10.0 ** rng.uniform(-2, 4, theta.size)
+    u = rng.normal(size=(theta.size, 3))
+    h = _pair_rounded(u / np.linalg.norm(u, axis=1)[:, None] * lam[:, None])
+    dl = _pair_rounded(theta / lam)
+    lib = xg.load()
+    cm, S = np.empty(theta.size), np.empty(theta.size)
+    rc = lib.xf_probe_df_propagator(theta.size, xg._dp(np.ascontiguousarray(h.reshape(-1))), xg._dp(dl), half,
+                                    xg._dp(cm), xg._dp(S))
+    assert rc == 0
+    q = 0.5 if half else 1.0
+    lam_r = np.sqrt(np.sum(h * h, axis=1))
+    th = lam_r * dl
+    cm_ref = -2.0 * q * np.sin(0.5 * th) ** 2
+    S_ref = q * np.sin(th) / lam_r
+    tol = 1e-14 + 4e-14 * th
+    assert np.all(np.abs(cm - cm_ref) <= q * tol), np.max(np.abs(cm - cm_ref) / tol)
+    assert np.all(np.abs(S - S_ref) <= q * dl * tol), np.max(np.abs(S - S_ref) / (dl * tol))
 
 
 @pytest.mark.parametrize("r0,iters", [(10.0, 400), (50.0, 300)])

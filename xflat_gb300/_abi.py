@@ -91,6 +91,8 @@ PROTOTYPES = {
     "xf_phase_times": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_long_p]),
     "xf_survival": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "xf_probe_fp64_peak": (ctypes.c_int, [ctypes.c_double, c_double_p]),
+    "xf_probe_df_propagator": (ctypes.c_int, [ctypes.c_int, c_double_p, c_double_p, ctypes.c_int, c_double_p,
+                                              c_double_p]),
     "xf_calc_hvv_static": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_double_p,

@@ -16,7 +16,10 @@
 // pairs; when t <= 1e-3 in the whole warp (the bulb run's steps) the rest of
 // c1 and s1 is an FP32 tail, which with the FP32 rounding of t in it changes
 // C and S by less than 5e-15 (3.1e-15 at t = 1e-3), otherwise the series is
-// a pair Horner up to t = 0.25 and FP64 sincos beyond.
+// a pair Horner up to t = 0.25; beyond, the angle |h| dl is reduced by
+// multiples of pi/2 in pairs and the remainder's series rotated by the
+// quadrant (no FP64 sincos: the first step of a run from 10 km, dl = 1e-3
+// km across a matter potential up to 1e4 /km, takes this branch in most bins).
 //
 // Arithmetic.  Intermediate values are "loose" pairs: the hi parts of
 // products and sums are exact error-free transformations (TwoProduct with
@@ -166,17 +169,41 @@ struct DConst {
     float h, l;
 };
 #define XF_DFC(v) DConst{(float)(v), (float)((v) - (double)(float)(v))}
-__constant__ DConst kDC[7] = {XF_DFC(-1.0 / 2.0),      XF_DFC(1.0 / 24.0),        XF_DFC(-1.0 / 720.0),
+__constant__ DConst kDC[8] = {XF_DFC(-1.0 / 2.0),      XF_DFC(1.0 / 24.0),        XF_DFC(-1.0 / 720.0),
                               XF_DFC(1.0 / 40320.0),   XF_DFC(-1.0 / 3628800.0),  XF_DFC(1.0 / 479001600.0),
-                              XF_DFC(-1.0 / 87178291200.0)};
-__constant__ DConst kDS[7] = {XF_DFC(-1.0 / 6.0),         XF_DFC(1.0 / 120.0),          XF_DFC(-1.0 / 5040.0),
+                              XF_DFC(-1.0 / 87178291200.0), XF_DFC(1.0 / 20922789888000.0)};
+__constant__ DConst kDS[8] = {XF_DFC(-1.0 / 6.0),         XF_DFC(1.0 / 120.0),          XF_DFC(-1.0 / 5040.0),
                               XF_DFC(1.0 / 362880.0),     XF_DFC(-1.0 / 39916800.0),    XF_DFC(1.0 / 6227020800.0),
-                              XF_DFC(-1.0 / 1307674368000.0)};
+                              XF_DFC(-1.0 / 1307674368000.0), XF_DFC(1.0 / 355687428096000.0)};
 #undef XF_DFC
 constexpr float kS1h = (float)(-1.0 / 6.0);
 constexpr float kS1l = (float)(-1.0 / 6.0 - (double)(float)(-1.0 / 6.0));
 
 __device__ __forceinline__ DF dconst(const DConst& c) { return DF{c.h, c.l}; }
+
+// pi/2 as three floats (their sum is pi/2 to 1.1e-23; each product with an
+// integer n < 2^24 is an exact pair), and 2/pi rounded to FP32.
+constexpr float kPio2a = 0x1.921fb6p+0f, kPio2b = -0x1.777a5cp-25f, kPio2c = -0x1.ee59dap-50f;
+constexpr float kTwoOverPi = 0x1.45f306p-1f;
+
+// Square root of a normalised pair a > 0: the FP32 root s and one correction
+// (a - s^2) / 2s from the residual, whose leading term an FMA forms exactly
+// (Dekker's double-length square root, 1971).
+__device__ __forceinline__ DF dsqrt(const DF& a)
+{
+    const float s = __fsqrt_rn(a.h);
+    const float e = fmaf(-s, s, a.h) + a.l;
+    return norm(DF{s, __fdividef(e, s + s)});
+}
+
+// 1/a for a normalised pair a != 0: the FP32 reciprocal r and one Newton
+// correction r (1 - a r), the residual formed with FMAs.
+__device__ __forceinline__ DF drcp(const DF& a)
+{
+    const float r = __frcp_rn(a.h);
+    const float e = fmaf(-a.l, r, fmaf(-a.h, r, 1.f));
+    return norm(DF{r, r * e});
+}
 
 // Coefficients of U over dl for the bin Hamiltonian (h00, h01r, beam h01i).
 // Must be called by all 32 lanes of the warp (warp-uniform series choice).
@@ -216,12 +243,43 @@ __device__ __forceinline__ DK dcoeffs(const DF& h00, const DF& h01r, const DF& h
         const DF dl = norm(bm.dl);
         k.S = dscale(q, df_add(dl, df_mul(dl, df_mul(tn, s1))));
     } else {
-        const double lam = sqrt(df_value(lam2));
-        const double dl = df_value(bm.dl);
-        double sn, cs;
-        sincos(lam * dl, &sn, &cs);
-        k.cm = dsplit(q * (cs - 1.0));
-        k.S = dsplit(q * (sn / lam));
+        // theta = sqrt(t) = |h| dl less the nearest multiple n pi/2 (Cody and
+        // Waite's reduction with the three-float pi/2, in pairs: the remainder
+        // keeps theta's own absolute precision, 2^-47 theta), |r| <= pi/4 +
+        // 1e-3; cos r - 1 and sin r from the pair series to degree 8 in r^2
+        // (truncation below 4e-18), rotated by the quadrant n mod 4:
+        // cos(theta) - 1 and sin(theta), and S = q sin(theta) dl / theta
+        const DF th = dsqrt(norm(t));
+        const float n = rintf(th.h * kTwoOverPi);
+        DF r = df_add(th, neg(two_prod(n, kPio2a)));
+        r = df_add(r, neg(two_prod(n, kPio2b)));
+        r = df_add(r, DF{-n * kPio2c, 0.f});
+        const DF u = df_mul(r, r);
+        DF c1 = dconst(kDC[7]), s1 = dconst(kDS[7]);
+#pragma unroll
+        for (int i = 6; i >= 0; --i) {
+            c1 = df_add(dconst(kDC[i]), df_mul(c1, u));
+            s1 = df_add(dconst(kDS[i]), df_mul(s1, u));
+        }
+        const DF cr = df_mul(u, c1);                          // cos r - 1
+        const DF sr = df_add(r, df_mul(r, df_mul(u, s1)));  // sin r
+        const int quad = (int)n & 3;
+        DF cm, sn;
+        if (quad == 0) {
+            cm = cr;
+            sn = sr;
+        } else if (quad == 1) {
+            cm = df_add(DF{-1.f, 0.f}, neg(sr));
+            sn = df_add(DF{1.f, 0.f}, cr);
+        } else if (quad == 2) {
+            cm = df_add(DF{-2.f, 0.f}, neg(cr));
+            sn = neg(sr);
+        } else {
+            cm = df_add(DF{-1.f, 0.f}, sr);
+            sn = neg(df_add(DF{1.f, 0.f}, cr));
+        }
+        k.cm = dscale(q, cm);
+        k.S = dscale(q, df_mul(df_mul(sn, norm(bm.dl)), drcp(th)));
     }
     return k;
 }

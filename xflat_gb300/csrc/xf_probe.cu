@@ -1,6 +1,8 @@
-// FP64 FMA throughput probe: the denominator of the FP64-pipe roofline.
+// Probes: the FP64 FMA throughput (the denominator of the FP64-pipe
+// roofline) and the double-float propagator coefficients on given inputs.
 #include <cuda_runtime.h>
 
+#include "xf_df.cuh"
 #include "xflat_gpu.h"
 
 namespace {
@@ -57,4 +59,44 @@ extern "C" int xf_probe_fp64_peak(double ms, double* tflops)
     if (err != cudaSuccess || t <= 0.f) return XF_ECUDA;
     *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (t * 1e-3) / 1e12;
     return XF_OK;
+}
+
+// ------------------------------------------------------------------ double-float propagator
+
+namespace {
+
+__global__ void k_df_propagator(int n, const double* __restrict__ h, const double* __restrict__ dl, int half,
+                                double* __restrict__ cm, double* __restrict__ S)
+{
+    using namespace xf::dfp;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = i < n ? i : n - 1;  // lanes past n repeat the last input: every lane takes part
+    const DF h00 = dsplit(h[3 * j]), h01r = dsplit(h[3 * j + 1]), h01i = dsplit(h[3 * j + 2]);
+    const DLen bm = dlen(dsplit(dl[j]));
+    const DK k = half ? dcoeffs<1>(h00, h01r, dsq(h01i), bm) : dcoeffs<0>(h00, h01r, dsq(h01i), bm);
+    if (i < n) {
+        cm[i] = df_value(k.cm);
+        S[i] = df_value(k.S);
+    }
+}
+
+}  // namespace
+
+extern "C" int xf_probe_df_propagator(int n, const double* h, const double* dl, int half, double* cm, double* S)
+{
+    if (n <= 0 || !h || !dl || !cm || !S) return XF_EINVAL;
+    double* d = nullptr;
+    const size_t nb = (size_t)n * sizeof(double);
+    if (cudaMalloc(&d, 6 * nb) != cudaSuccess) return XF_ENOMEM;
+    double *dh = d, *ddl = d + 3 * (size_t)n, *dcm = d + 4 * (size_t)n, *dS = d + 5 * (size_t)n;
+    cudaError_t err = cudaMemcpy(dh, h, 3 * nb, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(ddl, dl, nb, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) {
+        k_df_propagator<<<(n + 255) / 256, 256>>>(n, dh, ddl, half, dcm, dS);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpy(cm, dcm, nb, cudaMemcpyDeviceToHost);
+    if (err == cudaSuccess) err = cudaMemcpy(S, dS, nb, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return err == cudaSuccess ? XF_OK : XF_ECUDA;
 }
