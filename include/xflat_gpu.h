@@ -147,7 +147,7 @@ int xf_dims(const xf_handle* h, int* nbeams, int* ebins, int* abins, int* pbins)
  * (default 16, 0 = never; the double-float path takes 0 only); "prefetch"
  * sets how many energy-loop iterations ahead the mixed and double-float phase
  * kernels prefetch the state rows into L1 (default 1, 0 = none);
- * "df_b_occupancy" (2 or 3, default 2) picks the double-float phase-B kernel
+ * "df_b_occupancy" (2 or 3, default 3) picks the double-float phase-B kernel
  * built for that many resident blocks per SM; "persistent" (1, 0, or -1 for
  * the default choice by size and precision) runs a device-controlled xf_run
  * of FP64 or double-float as one cooperative launch per iters_per_launch

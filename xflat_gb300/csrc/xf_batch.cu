@@ -82,7 +82,7 @@ constexpr int batch_min_blocks()
 {
     return PREC == XF_PREC_FP64    ? (PH == xf::PH_C ? 3 : 1)
            : PREC == XF_PREC_MIXED ? (PH == xf::PH_A ? 5 : (PH == xf::PH_B ? 6 : 4))
-                                   : (PH == xf::PH_B ? 2 : 3);
+                                   : 3;
 }
 
 template <int PREC, int PH>

@@ -12,9 +12,9 @@ namespace {
 
 using namespace detail;
 
-// 3 resident blocks of 256 threads per SM (at most 85 registers per thread);
-// phase B, which holds two propagators' constants, also in a form with 2
-// (128 registers, no spills)
+// 3 resident blocks of 256 threads per SM (at most 85 registers per thread,
+// no spills); phase B, which holds two propagators' constants, also in a form
+// with 2 (128 registers), 7 % slower on GB300
 constexpr int kDfMinBlocks = 3;
 
 template <int GEOM>

@@ -12,7 +12,7 @@ struct Shape {
     int blocks = 0;      // grid size of the phase kernels
     int blocks_ab = 0;   // mixed precision: grid size of phases A and B (0: blocks)
     int phase_blocks[3] = {0, 0, 0};  // double-float: grid size of phases A, B, C (0: blocks)
-    int df_b_occ = 2;    // double-float: resident blocks per SM of the phase-B kernel (2 or 3)
+    int df_b_occ = 3;    // double-float: resident blocks per SM of the phase-B kernel (2 or 3)
     int fp64_fused = 1;  // FP64: averages folded into the FMA chains of phases B and C (0: separate additions)
 };
 
