@@ -13,7 +13,8 @@ instances (124 K to 242 K bins each, mixed hierarchies and luminosities) run
 from r = 50 km to their final radius of 600 km as one double-float batch and
 one FP64 batch, compared the same way at 600 km.
 
-Bars: double-float within 1e-5 of FP64 (the spec bar).  A batch
+Bars: double-float within 1e-5 of FP64 (the accuracy target of the faster
+variants).  A batch
 instance that misses it free-running is examined: FP64's own accepted steps
 replayed in double-float, and FP64 with the tolerance moved by 1e-4 relative;
 on such an ill-conditioned trajectory the replayed difference must stay

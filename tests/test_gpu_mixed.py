@@ -1,7 +1,7 @@
 """Mixed-precision path (FP32 rotations and compensated FP32 state; FP64
 reductions, error estimate, control and renormalisation) against the FP64 path.
 Bars: P_ee(E) of every nu_e beam within 1e-5 of FP64 over the windows below
-(the spec bar for the mixed path); the step error within 2e-2 relative at step sizes near the adaptive ones."""
+(the accuracy target of the faster variants); the step error within 2e-2 relative at step sizes near the adaptive ones."""
 import numpy as np
 import pytest
 
