@@ -3,6 +3,7 @@ config parsing with the reference's units, tables, matter, initial state, and
 the exported symbol set."""
 import ctypes
 import os
+import re
 
 import numpy as np
 import pytest
@@ -145,3 +146,33 @@ def test_double_float_series_fast_path():
         worst_c = max(worst_c, abs(float(mp.cos(x) - 1 - cm)))
         worst_s = max(worst_s, abs(float(mp.sin(x) / x - 1 - sm)))
     assert worst_c <= 5e-15 and worst_s <= 5e-15, (worst_c, worst_s)
+
+
+def test_double_float_large_angle_constants():
+    """The double-float propagator's large-angle branch (xflat_gb300/csrc/
+    xf_df.cuh, dcoeffs, t > 0.25): pi/2 as three FP32 numbers whose sum is
+    pi/2 to 1.1e-23 (each product with an integer n < 2^24 is then an exact
+    pair), 2/pi rounded to FP32, and the series of the remainder (|r| <=
+    pi/4 + 1e-3) truncated below 4e-18: cos r - 1 after the u^8 term and
+    sin r after the r u^8 term (u = r^2), the first omitted terms u^9/18!
+    and r u^9/19!."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 50
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "xflat_gb300", "csrc",
+                            "xf_df.cuh")).read()
+    hexf = r"(-?0x[0-9a-f.]+p[-+]?\d+)f"
+    m = re.search(r"kPio2a = %s, kPio2b = %s, kPio2c = %s" % (hexf, hexf, hexf), src)
+    assert m, "pi/2 split not found"
+    parts = [float.fromhex(x) for x in m.groups()]
+    for x in parts:
+        assert float(np.float32(x)) == x
+    assert abs(sum(mp.mpf(x) for x in parts) - mp.pi / 2) < mp.mpf("1.1e-23")
+    m = re.search(r"kTwoOverPi = %s" % hexf, src)
+    assert m and float.fromhex(m.group(1)) == float(np.float32(float(2 / mp.pi)))
+    r = mp.pi / 4 + mp.mpf("1e-3")
+    u = r * r
+    assert u ** 9 / mp.factorial(18) < mp.mpf("4e-18")
+    assert r * u ** 9 / mp.factorial(19) < mp.mpf("4e-18")
+    # the kernel's coefficient tables run to 1/16! and 1/17! (index 7)
+    assert "XF_DFC(1.0 / 20922789888000.0)" in src and "XF_DFC(1.0 / 355687428096000.0)" in src
+    assert mp.factorial(16) == 20922789888000 and mp.factorial(17) == 355687428096000
