@@ -309,11 +309,6 @@ __device__ inline bool group_reduce_tail(const RedTarget& rt, int nused, double 
     return true;
 }
 
-// The step controller of src/Nmr.cpp:227-249 under device control, run by one
-// thread after Max_err is known: accept (r += dr, psi0 <-> psi4, S0 <-> S4,
-// J0 <- JC, record the step), count the iteration, update dr with the
-// reference's formula and clamps, and decide whether the loop ends.  Returns
-// true when the step was accepted.
 // The 8 bytes of v in reverse order: the halves swapped, each byte-reversed
 // (a double in the NetCDF file's big-endian encoding on a little-endian GPU).
 __device__ __forceinline__ double byte_reversed(double v)
@@ -322,12 +317,6 @@ __device__ __forceinline__ double byte_reversed(double v)
     return __hiloint2double((int)__byte_perm(lo, 0, 0x0123), (int)__byte_perm(hi, 0, 0x0123));
 }
 
-// Staging of one beam of psi0 for a record decided by the step controller
-// (one warp): the Snapshot slot receives the beam's four components, unpadded
-// and big-endian; the Probability slot its survival sum_e fv (ar^2 + ai^2)
-// with the spectrum of particle p % 2 (src/IO_f.cpp:341-351), reduced in the
-// order of the stand-alone output kernels so both routes write the same
-// bits.  psi is the FP64 state, or null for the compensated pair (hi, lo).
 // Component k of energy bin e of beam b of a compensated-pair state (hi, lo)
 // as a double: the mixed path's rows ([beam][comp][epad] hi and lo arrays)
 // or, for the double-float path (d.df), its bin layout ([beam][epad][8]
@@ -342,6 +331,12 @@ __device__ __forceinline__ double pair_at(const Dev& d, const float* hi, const f
     return (double)hi[i] + (double)lo[i];
 }
 
+// Staging of one beam of psi0 for a record decided by the step controller
+// (one warp): the Snapshot slot receives the beam's four components, unpadded
+// and big-endian; the Probability slot its survival sum_e fv (ar^2 + ai^2)
+// with the spectrum of particle p % 2 (src/IO_f.cpp:341-351), reduced in the
+// order of the stand-alone output kernels so both routes write the same
+// bits.  psi is the FP64 state, or null for the compensated pair (hi, lo).
 __device__ inline void stage_beam(const Dev& d, const Ctl* ctl, int kind, int b, int lane, const double* psi,
                                   const float* hi, const float* lo)
 {
@@ -457,6 +452,11 @@ __device__ inline void io_triggers(const Dev& d, Ctl* ctl, double r, double dr, 
     }
 }
 
+// The step controller of src/Nmr.cpp:227-249 under device control, run by one
+// thread after Max_err is known: accept (r += dr, psi0 <-> psi4, S0 <-> S4,
+// J0 <- JC, record the step), count the iteration, update dr with the
+// reference's formula and clamps, and decide whether the loop ends.  Returns
+// true when the step was accepted.
 __device__ inline bool step_control(const Dev& d, Ctl* ctl, double me)
 {
     double r = ctl->r, dr = ctl->dr;
