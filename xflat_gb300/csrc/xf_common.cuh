@@ -182,11 +182,6 @@ __device__ __forceinline__ void add_moment_lane(const Dev& d, double val, int z,
 // Value slot v of a phase -> (stage point, density component) of the moment it feeds.
 __device__ __forceinline__ int comp_of(int k) { return k == 0 ? 0 : (k == 1 ? 2 : 3); }
 
-// Block-level combination of per-lane moment accumulators followed by the
-// last-block reduction over the group's blocks.  Lanes l with l % G == 0 (G = 32/NV) own
-// value v = l / G; values v < nused feed moments.  Returns true in the last
-// block, with s_out[0..nused*K) holding the grid totals and s_out[31] the grid
-// maximum of `mx` (ignored unless with_max).
 // Where a group of blocks reduces its per-block partials: the block's slot
 // `idx` of `count` slots at `partials` (followed by room for the group sums,
 // red_rows(count) rows in all), the tickets that elect the last block of each
@@ -204,6 +199,11 @@ template <int K>
 __device__ inline bool group_reduce_tail(const RedTarget& rt, int nused, double mx, bool with_max, double* s_warp,
                                          double* s_out);
 
+// Block-level combination of per-lane moment accumulators followed by the
+// last-block reduction over the group's blocks.  Lanes l with l % G == 0 (G = 32/NV) own
+// value v = l / G; values v < nused feed moments.  Returns true in the last
+// block, with s_out[0..nused*K) holding the grid totals and s_out[31] the grid
+// maximum of `mx` (ignored unless with_max).
 template <int K>
 __device__ inline bool group_reduce(const RedTarget& rt, int G, int nused, const double (&acc)[K], double mx,
                                     bool with_max, double* s_warp, double* s_out)
