@@ -239,7 +239,7 @@ int xf_probe_fp64_peak(double ms, double* tflops);
  * pairs, evaluated on the device by the double-float kernels' own code, with
  * q = 1/2 when `half` is set, else 1.  Returns cm[i] = q (cos(|h| dl) - 1)
  * and S[i] = q sin(|h| dl) / |h| (host arrays).  The series branch is chosen
- * per warp of 32 consecutive inputs, as in the kernels. */
+ * per warp of 32 consecutive inputs, as in the kernels.  1 <= n <= 2^26. */
 int xf_probe_df_propagator(int n, const double* h, const double* dl, int half, double* cm, double* S);
 
 /* ---------------------------------------------------------------- files */

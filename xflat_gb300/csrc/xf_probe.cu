@@ -84,7 +84,7 @@ __global__ void k_df_propagator(int n, const double* __restrict__ h, const doubl
 
 extern "C" int xf_probe_df_propagator(int n, const double* h, const double* dl, int half, double* cm, double* S)
 {
-    if (n <= 0 || !h || !dl || !cm || !S) return XF_EINVAL;
+    if (n <= 0 || n > (1 << 26) || !h || !dl || !cm || !S) return XF_EINVAL;
     double* d = nullptr;
     const size_t nb = (size_t)n * sizeof(double);
     if (cudaMalloc(&d, 6 * nb) != cudaSuccess) return XF_ENOMEM;
